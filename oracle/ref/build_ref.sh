@@ -1,0 +1,17 @@
+#!/bin/bash
+# Builds the UNMODIFIED reference engine + ref_harness.cpp into oracle/_ref/.
+# Runs only where the reference sources are present (not on the GPU machine) and
+# only on x86-64 with AVX-512 (the reference uses AVX-512 intrinsics and x86 asm).
+set -e
+HERE="$(cd "$(dirname "$0")" && pwd)"
+SRC="${PROTH_REF_SRC:-/root/reference/prothlogic4.2}"
+OUT="$HERE/../_ref"
+[ -d "$SRC" ] || { echo "reference sources not found: $SRC"; exit 1; }
+[ "$(uname -m)" = "x86_64" ] || { echo "reference needs x86-64 (AVX-512)"; exit 1; }
+mkdir -p "$OUT"
+# SETUP:25 flags, without -lgmpxx/-lcufft (unused on this path)
+FLAGS="-O3 -march=native -mavx512f -mfma -funroll-loops -fomit-frame-pointer -mprefer-vector-width=512 -ffast-math -std=c++17 -pthread"
+g++ $FLAGS -I"$HERE/gmpstub" -I"$SRC" -o "$OUT/ref_harness" \
+    "$HERE/ref_harness.cpp" "$SRC/fft_engine.cpp" "$SRC/llr_fft_pack.cpp" "$SRC/checkpoint_manager.cpp" \
+    "$SRC/proth_logic.cpp" "$SRC/storage_core.cpp" -l:libgmp.so.10 -w
+echo "built $OUT/ref_harness"
