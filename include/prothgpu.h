@@ -1,0 +1,151 @@
+/*
+ * prothgpu.h -- C ABI of the GB300 Proth modular-squaring engine (libprothgpu.so).
+ *
+ * Plain C types only (no CUDA or C++ types), so cgo, JNI, ctypes or the
+ * reference's own C++ can bind it.  Residues cross the boundary as
+ * little-endian 64-bit limbs, the layout of the reference's limb buffers
+ * (prothlogic4.2/dcore.cpp:143-155, mpz_export order -1 at proth_logic.cpp:446).
+ *
+ * Every function returns a PG_* status; none aborts the process.  One engine
+ * handle belongs to one host thread at a time (the reference keeps one
+ * FFTContext per worker thread, dcore.cpp:134); distinct handles may be used
+ * from distinct threads concurrently, each on its own CUDA stream.
+ */
+#ifndef PROTHGPU_H
+#define PROTHGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define PG_OK 0
+#define PG_EINVAL 1     /* bad argument */
+#define PG_ENOMEM 2     /* device or host allocation failed */
+#define PG_EROUNDOFF 3  /* max |x - round(x)| > 0.4 at the largest FFT length allowed */
+#define PG_EGERBICZ 4   /* Gerbicz check kept failing after the allowed rollbacks */
+#define PG_ETIMEOUT 5   /* a bounded wait expired */
+#define PG_ECUDA 6      /* CUDA runtime error */
+#define PG_EIO 7        /* checkpoint file error */
+#define PG_ENODEV 8     /* no usable sm_103 device */
+#define PG_ESTATE 9     /* handle not ready for this call */
+#define PG_EOVERFLOW 10 /* a digit or carry left its representable range */
+
+/* pg_create flags */
+#define PG_FLAG_NO_GERBICZ 0x1u   /* skip the Gerbicz check in pg_square */
+#define PG_FLAG_NO_BUMP 0x2u      /* report PG_EROUNDOFF instead of growing the FFT */
+#define PG_FLAG_NO_GRAPH 0x4u     /* launch kernels directly instead of replaying a CUDA graph */
+#define PG_FLAG_FORCE_LEN 0x8u    /* use fft_len_hint exactly, even below the safe length (tests) */
+
+typedef struct pg_engine pg_engine;
+typedef struct pg_batch pg_batch;
+
+/* Result of one Proth test. */
+typedef struct pg_result {
+    uint64_t k;
+    uint32_t n;
+    uint32_t base;          /* a with Jacobi(a, N) = -1; 0 when the small-prime gate rejected N */
+    int32_t verdict;        /* 1: a^((N-1)/2) = -1 (prime), 0: composite */
+    int32_t status;         /* PG_* */
+    uint64_t res64;         /* limb 0 of a^((N-1)/2) mod N (0 when gated) */
+    uint64_t tag;           /* caller's tag (batch) */
+    uint32_t fft_len;       /* complex FFT length used at the end */
+    uint32_t fft_bumps;     /* FFT-length increases after roundoff > 0.4 */
+    uint32_t gerbicz_checks;
+    uint32_t gerbicz_failures;
+    double max_err;         /* largest max |x - round(x)| seen */
+    double seconds;         /* time to verdict: submit (or call) to verdict */
+} pg_result;
+
+/* ---- library ---- */
+const char* pg_strerror(int status);
+int pg_version(void);                 /* 100 * major + minor */
+int pg_device_info(char* name, size_t name_len, int* sm_count);
+/* FFT length (complex points) the engine picks for k*2^n+1; 0 if n is out of range. */
+uint32_t pg_pick_fft_len(uint64_t k, uint32_t n);
+
+/* Host-only pieces of the Proth test (no device needed). */
+/* 1 if a gate prime <= 67 divides k*2^n+1 (is_divisible_by_gate, proth_logic.cpp:41-50, 400-408). */
+int pg_gate_rejects(uint64_t k, uint32_t n);
+/* Smallest listed base a with Jacobi(a, N) = -1, else 0 (proth_logic.cpp:411-422). */
+uint64_t pg_choose_base(uint64_t k, uint32_t n);
+/* Device representation round trip on the host: x -> Montgomery form -> M
+ * balanced digits -> value -> x mod N.  Returns PG_OK and the canonical x. */
+int pg_host_roundtrip(uint64_t k, uint32_t n, uint32_t M, const uint64_t* x, size_t n_limbs, uint64_t* out,
+                      size_t out_limbs);
+
+/* ---- single-candidate engine (all SMs on one residue) ----
+ * Replaces fft_init / fft_destroy / fft_square_karatsuba
+ * (prothlogic4.2/fft_engine.h:10-22, fft_engine.cpp:18-80 and 986-1073) and the
+ * reduction the reference loop runs after each squaring (proth_logic.cpp:488-533).
+ * The residue stays on the device between calls; pg_set_residue /
+ * pg_get_residue move it across the boundary. */
+int pg_create(uint64_t k, uint32_t n, uint32_t fft_len_hint, uint32_t flags, pg_engine** out);
+int pg_destroy(pg_engine* e);
+/* x (n_limbs little-endian limbs, any value) is reduced mod N and loaded. */
+int pg_set_residue(pg_engine* e, const uint64_t* limbs, size_t n_limbs);
+/* Canonical x mod N into n_limbs limbs (zero-padded); n_limbs >= ceil((n + 64)/64). */
+int pg_get_residue(pg_engine* e, uint64_t* limbs, size_t n_limbs);
+/* x <- x^(2^iters) mod N.  Each squaring records max |x - round(x)|; above 0.4
+ * the engine rolls back to its last verified residue and grows the FFT length.
+ * A Gerbicz check covers every block of squarings unless PG_FLAG_NO_GERBICZ. */
+int pg_square(pg_engine* e, uint64_t iters);
+/* x <- base_a^exponent mod N by left-to-right binary powering on the device
+ * (x <- x^2 * a^bit per step); used for x0 = a^k (proth_logic.cpp:424-446). */
+int pg_pow_small(pg_engine* e, uint64_t base_a, uint64_t exponent);
+/* Largest roundoff error since the last reset (ctx.last_max_diff). */
+int pg_max_err(pg_engine* e, double* out, int reset);
+int pg_fft_len(const pg_engine* e, uint32_t* out);
+/* Gerbicz block length in squarings (default 1000) and verification interval
+ * in blocks (default 0 = verify at the end of every pg_square call). */
+int pg_set_gerbicz(pg_engine* e, uint32_t block, uint32_t verify_every_blocks);
+/* Counters: squarings done, Gerbicz checks, failures, FFT bumps. */
+int pg_stats(const pg_engine* e, uint64_t* squarings, uint32_t* checks, uint32_t* failures,
+             uint32_t* bumps);
+/* Device-timed run of `iters` squarings (CUDA events on the engine's stream,
+ * graph replay, no rollback bookkeeping); *ms receives the elapsed time.  The
+ * residue advances by `iters` squarings.  Returns the launches per squaring in
+ * *kernels_per_step. */
+int pg_time_squarings(pg_engine* e, uint64_t iters, double* ms, uint32_t* kernels_per_step);
+/* Per-kernel device times (ms) of one squaring, launched one by one with an
+ * event pair around each: times[i] for i < *count (at most cap). */
+int pg_profile_step(pg_engine* e, double* times, uint32_t cap, uint32_t* count);
+/* Test hook: add `delta` to residue digit `index` on the device (simulates a
+ * silent memory error; nothing faults).  Used by the failure-detection tests. */
+int pg_debug_corrupt(pg_engine* e, uint32_t index, int32_t delta);
+
+/* Checkpoint file in the reference format (checkpoint_manager.h:10-16):
+ * {uint64 current_i, size_t n_limbs} + n_limbs limbs, followed by an extension
+ * block (k, n, FFT length, squarings completed, checksum) that the reference
+ * reader ignores.  current_i keeps the reference meaning: index of the last
+ * completed squaring of the test loop. */
+int pg_checkpoint_save(pg_engine* e, const char* path, uint64_t current_i);
+int pg_checkpoint_load(pg_engine* e, const char* path, uint64_t* current_i);
+
+/* Full Proth test on the device: the gate of proth_logic.cpp:400-408, base
+ * choice :411-422, x0 = a^k mod N, n-1 squarings, verdict x == N-1
+ * (execute_proth_test_fft, proth_logic.cpp:384-580). */
+int pg_proth_test(uint64_t k, uint32_t n, uint32_t flags, pg_result* out);
+
+/* ---- batched engine: many candidates per launch, grouped by FFT length ----
+ * Replaces the reference's worker pool (dcore.cpp:84-193 dispatch with
+ * worker.cpp:27-69 run_task_with_ctx over PROTH_FF_BATCH k lists). */
+int pg_batch_create(uint32_t max_slots_per_class, uint32_t flags, pg_batch** out);
+int pg_batch_destroy(pg_batch* b);
+/* Queue one candidate; the gate and base choice run on the host at submit. */
+int pg_batch_submit(pg_batch* b, uint64_t k, uint32_t n, uint64_t tag);
+/* Advance every admitted candidate by up to `max_steps` squarings (0: until
+ * all queued candidates are done), admitting queued ones into free slots. */
+int pg_batch_run(pg_batch* b, uint64_t max_steps);
+/* Move up to `cap` finished results out; *count receives how many. */
+int pg_batch_poll(pg_batch* b, pg_result* out, size_t cap, size_t* count);
+/* Queued, running and finished-but-unpolled candidate counts. */
+int pg_batch_pending(const pg_batch* b, size_t* queued, size_t* running, size_t* finished);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,7 +1,7 @@
 // Test harness around the UNMODIFIED reference engine (compiled from the
 // reference sources by build_ref.sh into oracle/_ref/).  Test infrastructure only.
 //
-//   ref_harness trace <k> <n> <L> <steps> <x0_hex>
+//   ref_harness trace <k> <n> <L> <steps> <x0_hex | - (hex on stdin)>
 //       runs <steps> reference squarings (fft_square_karatsuba, fft_engine.cpp:986)
 //       at FFT length L from x0, canonicalising each step with GMP mpz_mod, and
 //       prints "i res64 maxerr" per step.
@@ -12,6 +12,7 @@
 //       engine-only microseconds per squaring.
 #include "fft_engine.h"
 #include "proth_logic.h"
+#include <cctype>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -51,7 +52,17 @@ int main(int argc, char** argv) {
     }
     if (mode == "trace" || mode == "time") {
         unsigned long steps = strtoul(argv[5], nullptr, 10);
-        std::vector<uint64_t> x0 = (mode == "trace") ? parse_hex(argv[6], nl) : std::vector<uint64_t>(nl, 0);
+        std::vector<uint64_t> x0(nl, 0);
+        if (mode == "trace") {
+            std::string hex = argv[6];
+            if (hex == "-") {  // read the hex residue from standard input
+                hex.clear();
+                int ch;
+                while ((ch = getchar()) != EOF)
+                    if (isxdigit(ch)) hex.push_back((char)ch);
+            }
+            x0 = parse_hex(hex.c_str(), nl);
+        }
         if (mode == "time") for (size_t i = 0; i < n / 64; ++i) x0[i] = 0x9E3779B97F4A7C15ULL * (i + 1);
         memcpy(limbs.data(), x0.data(), nl * 8);
         mpz_t N, r;

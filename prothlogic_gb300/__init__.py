@@ -1,0 +1,277 @@
+"""prothlogic_gb300 -- GB300-native engine for the Proth modular-squaring path.
+
+The compute path is libprothgpu.so (hand-written sm_103a CUDA kernels + a C++
+host engine behind the C ABI declared in include/prothgpu.h).  This module is a
+thin ctypes binding that mirrors the reference's engine interface
+(prothlogic4.2/fft_engine.h: init for k,n / square / last_max_diff, and
+proth_logic.h: execute_proth_test_fft).  There is no CPU fallback: every call
+that needs the device raises ProthGpuError when the library or the GPU is
+missing.
+"""
+import ctypes
+import os
+
+from . import build as _build_mod
+
+__all__ = ["ProthGpuError", "Engine", "Batch", "proth_test", "execute_proth_test_fft",
+           "load", "pick_fft_len", "gate_rejects", "choose_base", "host_roundtrip"]
+
+PG_OK = 0
+PG_EROUNDOFF = 3
+PG_EGERBICZ = 4
+FLAG_NO_GERBICZ = 0x1
+FLAG_NO_BUMP = 0x2
+FLAG_NO_GRAPH = 0x4
+FLAG_FORCE_LEN = 0x8
+
+_u64 = ctypes.c_uint64
+_u32 = ctypes.c_uint32
+_i32 = ctypes.c_int32
+_vp = ctypes.c_void_p
+_sz = ctypes.c_size_t
+
+
+class PgResult(ctypes.Structure):
+    _fields_ = [("k", _u64), ("n", _u32), ("base", _u32), ("verdict", _i32), ("status", _i32),
+                ("res64", _u64), ("tag", _u64), ("fft_len", _u32), ("fft_bumps", _u32),
+                ("gerbicz_checks", _u32), ("gerbicz_failures", _u32), ("max_err", ctypes.c_double),
+                ("seconds", ctypes.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class ProthGpuError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        msg = _lib.pg_strerror(status).decode() if _lib is not None else str(status)
+        super().__init__(f"{what}: {msg} (status {status})" if what else msg)
+
+
+_lib = None
+
+# symbol name -> (restype, argtypes); the exported surface of include/prothgpu.h
+SIGNATURES = {
+    "pg_strerror": (ctypes.c_char_p, [ctypes.c_int]),
+    "pg_version": (ctypes.c_int, []),
+    "pg_device_info": (ctypes.c_int, [ctypes.c_char_p, _sz, ctypes.POINTER(ctypes.c_int)]),
+    "pg_pick_fft_len": (_u32, [_u64, _u32]),
+    "pg_gate_rejects": (ctypes.c_int, [_u64, _u32]),
+    "pg_choose_base": (_u64, [_u64, _u32]),
+    "pg_host_roundtrip": (ctypes.c_int, [_u64, _u32, _u32, ctypes.POINTER(_u64), _sz, ctypes.POINTER(_u64), _sz]),
+    "pg_create": (ctypes.c_int, [_u64, _u32, _u32, _u32, ctypes.POINTER(_vp)]),
+    "pg_destroy": (ctypes.c_int, [_vp]),
+    "pg_set_residue": (ctypes.c_int, [_vp, ctypes.POINTER(_u64), _sz]),
+    "pg_get_residue": (ctypes.c_int, [_vp, ctypes.POINTER(_u64), _sz]),
+    "pg_square": (ctypes.c_int, [_vp, _u64]),
+    "pg_pow_small": (ctypes.c_int, [_vp, _u64, _u64]),
+    "pg_max_err": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
+    "pg_fft_len": (ctypes.c_int, [_vp, ctypes.POINTER(_u32)]),
+    "pg_set_gerbicz": (ctypes.c_int, [_vp, _u32, _u32]),
+    "pg_stats": (ctypes.c_int, [_vp, ctypes.POINTER(_u64), ctypes.POINTER(_u32), ctypes.POINTER(_u32),
+                                ctypes.POINTER(_u32)]),
+    "pg_debug_corrupt": (ctypes.c_int, [_vp, _u32, _i32]),
+    "pg_time_squarings": (ctypes.c_int, [_vp, _u64, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_u32)]),
+    "pg_profile_step": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), _u32, ctypes.POINTER(_u32)]),
+    "pg_checkpoint_save": (ctypes.c_int, [_vp, ctypes.c_char_p, _u64]),
+    "pg_checkpoint_load": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_u64)]),
+    "pg_proth_test": (ctypes.c_int, [_u64, _u32, _u32, ctypes.POINTER(PgResult)]),
+    "pg_batch_create": (ctypes.c_int, [_u32, _u32, ctypes.POINTER(_vp)]),
+    "pg_batch_destroy": (ctypes.c_int, [_vp]),
+    "pg_batch_submit": (ctypes.c_int, [_vp, _u64, _u32, _u64]),
+    "pg_batch_run": (ctypes.c_int, [_vp, _u64]),
+    "pg_batch_poll": (ctypes.c_int, [_vp, ctypes.POINTER(PgResult), _sz, ctypes.POINTER(_sz)]),
+    "pg_batch_pending": (ctypes.c_int, [_vp, ctypes.POINTER(_sz), ctypes.POINTER(_sz), ctypes.POINTER(_sz)]),
+}
+
+
+def load(build_if_missing=True):
+    """Load libprothgpu.so (building it in-tree with nvcc when absent or stale)."""
+    global _lib
+    if _lib is None:
+        if build_if_missing:
+            _build_mod.build()
+        if not os.path.exists(_build_mod.LIB):
+            raise ProthGpuError(8, "libprothgpu.so is not built")
+        lib = ctypes.CDLL(_build_mod.LIB)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _check(rc, what):
+    if rc != PG_OK:
+        raise ProthGpuError(rc, what)
+
+
+def _to_limbs(x, nl):
+    arr = (_u64 * nl)()
+    for i in range(nl):
+        arr[i] = (x >> (64 * i)) & 0xFFFFFFFFFFFFFFFF
+    return arr
+
+
+def _from_limbs(arr):
+    v = 0
+    for i in reversed(range(len(arr))):
+        v = (v << 64) | int(arr[i])
+    return v
+
+
+def pick_fft_len(k, n):
+    return load().pg_pick_fft_len(k, n)
+
+
+def gate_rejects(k, n):
+    return bool(load().pg_gate_rejects(k, n))
+
+
+def choose_base(k, n):
+    return int(load().pg_choose_base(k, n))
+
+
+def host_roundtrip(k, n, M, x):
+    nl = max(1, (x.bit_length() + 63) // 64)
+    out_nl = n // 64 + 4
+    out = (_u64 * out_nl)()
+    _check(load().pg_host_roundtrip(k, n, M, _to_limbs(x, nl), nl, out, out_nl), "pg_host_roundtrip")
+    return _from_limbs(out)
+
+
+class Engine:
+    """One candidate k*2^n+1 on the whole GPU (fft_init / fft_square_karatsuba / fft_destroy)."""
+
+    _h = None
+
+    def __init__(self, k, n, fft_len_hint=0, flags=0):
+        lib = load()
+        h = _vp()
+        _check(lib.pg_create(k, n, fft_len_hint, flags, ctypes.byref(h)), "pg_create")
+        self._h = h
+        self.k, self.n = k, n
+        self.N = k * (1 << n) + 1
+        self._nl = n // 64 + 3
+
+    def close(self):
+        if self._h:
+            load().pg_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_residue(self, x):
+        nl = max(1, (int(x).bit_length() + 63) // 64)
+        _check(load().pg_set_residue(self._h, _to_limbs(int(x), nl), nl), "pg_set_residue")
+
+    def get_residue(self):
+        out = (_u64 * self._nl)()
+        _check(load().pg_get_residue(self._h, out, self._nl), "pg_get_residue")
+        return _from_limbs(out)
+
+    def square(self, iters=1):
+        _check(load().pg_square(self._h, iters), "pg_square")
+
+    def pow_small(self, base, exponent):
+        _check(load().pg_pow_small(self._h, base, exponent), "pg_pow_small")
+
+    def max_err(self, reset=False):
+        v = ctypes.c_double()
+        _check(load().pg_max_err(self._h, ctypes.byref(v), 1 if reset else 0), "pg_max_err")
+        return v.value
+
+    @property
+    def fft_len(self):
+        v = _u32()
+        _check(load().pg_fft_len(self._h, ctypes.byref(v)), "pg_fft_len")
+        return v.value
+
+    def set_gerbicz(self, block, verify_every_blocks=0):
+        _check(load().pg_set_gerbicz(self._h, block, verify_every_blocks), "pg_set_gerbicz")
+
+    def stats(self):
+        sq, c, f, b = _u64(), _u32(), _u32(), _u32()
+        _check(load().pg_stats(self._h, ctypes.byref(sq), ctypes.byref(c), ctypes.byref(f), ctypes.byref(b)),
+               "pg_stats")
+        return {"squarings": sq.value, "gerbicz_checks": c.value, "gerbicz_failures": f.value,
+                "fft_bumps": b.value}
+
+    def time_squarings(self, iters):
+        """Device-timed squarings (CUDA events on the engine stream): (ms, kernels per squaring)."""
+        ms, kps = ctypes.c_double(), _u32()
+        _check(load().pg_time_squarings(self._h, iters, ctypes.byref(ms), ctypes.byref(kps)), "pg_time_squarings")
+        return ms.value, kps.value
+
+    def profile_step(self):
+        """Per-kernel device times (ms) of one squaring, kernels launched one by one."""
+        arr = (ctypes.c_double * 8)()
+        cnt = _u32()
+        _check(load().pg_profile_step(self._h, arr, 8, ctypes.byref(cnt)), "pg_profile_step")
+        return [arr[i] for i in range(cnt.value)]
+
+    def debug_corrupt(self, index, delta):
+        _check(load().pg_debug_corrupt(self._h, index, delta), "pg_debug_corrupt")
+
+    def checkpoint_save(self, path, current_i):
+        _check(load().pg_checkpoint_save(self._h, os.fsencode(path), current_i), "pg_checkpoint_save")
+
+    def checkpoint_load(self, path):
+        ci = _u64()
+        _check(load().pg_checkpoint_load(self._h, os.fsencode(path), ctypes.byref(ci)), "pg_checkpoint_load")
+        return ci.value
+
+
+def proth_test(k, n, flags=0):
+    """Full Proth test on the GPU; returns the result record as a dict."""
+    r = PgResult()
+    _check(load().pg_proth_test(k, n, flags, ctypes.byref(r)), f"pg_proth_test(k={k}, n={n})")
+    return r.as_dict()
+
+
+def execute_proth_test_fft(k, n):
+    """Reference-shaped entry point (proth_logic.h:12): True when k*2^n+1 is a Proth prime."""
+    return proth_test(k, n)["verdict"] == 1
+
+
+class Batch:
+    """Many candidates per launch, grouped by FFT length (the reference's worker pool)."""
+
+    _h = None
+
+    def __init__(self, max_slots_per_class=256, flags=0):
+        h = _vp()
+        _check(load().pg_batch_create(max_slots_per_class, flags, ctypes.byref(h)), "pg_batch_create")
+        self._h = h
+
+    def close(self):
+        if self._h:
+            load().pg_batch_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def submit(self, k, n, tag=0):
+        _check(load().pg_batch_submit(self._h, k, n, tag), "pg_batch_submit")
+
+    def run(self, max_steps=0):
+        _check(load().pg_batch_run(self._h, max_steps), "pg_batch_run")
+
+    def poll(self, cap=4096):
+        arr = (PgResult * cap)()
+        cnt = _sz()
+        _check(load().pg_batch_poll(self._h, arr, cap, ctypes.byref(cnt)), "pg_batch_poll")
+        return [arr[i].as_dict() for i in range(cnt.value)]
+
+    def pending(self):
+        q, r, f = _sz(), _sz(), _sz()
+        _check(load().pg_batch_pending(self._h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(f)),
+               "pg_batch_pending")
+        return q.value, r.value, f.value

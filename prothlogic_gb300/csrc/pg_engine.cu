@@ -1,0 +1,903 @@
+// pg_engine.cu -- host side of libprothgpu: plans, slot pools, the C ABI.
+//
+// Counterparts in the reference (prothlogic4.2/):
+//   fft_init / fft_destroy (fft_engine.cpp:18-80)   -> pg_create / pg_destroy, plan + weight caches
+//   fft_square_karatsuba + reduce (fft_engine.cpp:986-1073, proth_logic.cpp:488-533) -> pg_square
+//   execute_proth_test_fft (proth_logic.cpp:384-580) -> pg_proth_test
+//   dispatch + worker batches (dcore.cpp:84-193, worker.cpp:27-69) -> pg_batch_*
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/prothgpu.h"
+#include "pg_bigint.h"
+#include "pg_kernels.cuh"
+
+namespace pg {
+
+#define PG_CK(call)                                          \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) {                             \
+            note_cuda_error(e_, #call, __LINE__);            \
+            return PG_ECUDA;                                 \
+        }                                                    \
+    } while (0)
+
+static thread_local char g_last_error[256];
+static void note_cuda_error(cudaError_t e, const char* what, int line) {
+    snprintf(g_last_error, sizeof(g_last_error), "%s (line %d): %s", what, line, cudaGetErrorString(e));
+}
+
+// ---------------------------------------------------------------------------
+// Plans: one per FFT length M (complex points).
+
+struct Plan {
+    PlanDev dev;
+    int Gmid_small, Gmid_big, Ginner_small, Ginner_big;
+    double2* mem = nullptr;
+};
+
+static const int kMinLg = 8, kMaxLg = 18;
+static const double kMinBitsPerDigit = 6.0;  // below this the run carries do not settle
+
+static bool plan_radices(int lg, int F[MAX_PASSES], int& P) {
+    switch (lg) {
+        case 8: P = 2; F[0] = 16; F[1] = 16; return true;
+        case 9: P = 2; F[0] = 16; F[1] = 32; return true;
+        case 10: P = 2; F[0] = 32; F[1] = 32; return true;
+        case 11: P = 2; F[0] = 32; F[1] = 64; return true;
+        case 12: P = 2; F[0] = 64; F[1] = 64; return true;
+        case 13: P = 2; F[0] = 64; F[1] = 128; return true;
+        case 14: P = 2; F[0] = 128; F[1] = 128; return true;
+        case 15: P = 3; F[0] = 32; F[1] = 32; F[2] = 32; return true;
+        case 16: P = 3; F[0] = 16; F[1] = 64; F[2] = 64; return true;
+        case 17: P = 3; F[0] = 32; F[1] = 64; F[2] = 64; return true;
+        case 18: P = 3; F[0] = 64; F[1] = 64; F[2] = 64; return true;
+        default: return false;
+    }
+}
+
+// exp(-2 pi i num / den), from long double
+static double2 root_of_unity(uint64_t num, uint64_t den) {
+    num %= den;
+    const long double PI_L = 3.141592653589793238462643383279502884L;
+    const long double ang = -2.0L * PI_L * (long double)num / (long double)den;
+    return make_double2((double)cosl(ang), (double)sinl(ang));
+}
+
+// Stored position p -> frequency index, for smem_fft_fwd's stage order.
+static std::vector<int> stage_perm(int F) {
+    int lg = 0;
+    while ((1 << lg) < F) ++lg;
+    const int n4 = lg / 2;
+    std::vector<int> perm(F, 0);
+    for (int k = 0; k < F; ++k) {
+        int pos = 0, kk = k;
+        for (int s = 0; s < n4; ++s) {
+            pos += (kk % 4) * (F >> (2 * (s + 1)));
+            kk /= 4;
+        }
+        if (lg & 1) pos += kk % 2;
+        perm[pos] = k;
+    }
+    return perm;
+}
+
+static std::mutex g_cache_mu;
+static std::map<int, Plan*> g_plans;  // keyed by lgM (per process, current device)
+
+static int get_plan(int lg, Plan** out) {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    auto it = g_plans.find(lg);
+    if (it != g_plans.end()) {
+        *out = it->second;
+        return PG_OK;
+    }
+    Plan* p = new Plan();
+    PlanDev& d = p->dev;
+    memset(&d, 0, sizeof(d));
+    if (!plan_radices(lg, d.F, d.P)) {
+        delete p;
+        return PG_EINVAL;
+    }
+    d.M = 1 << lg;
+    d.lgM = lg;
+    int Mi = d.M;
+    for (int i = 0; i < d.P; ++i) {
+        d.Mi[i] = Mi;
+        d.S[i] = Mi / d.F[i];
+        Mi = d.S[i];
+    }
+    // host tables: inter-pass twiddles for i < P-1, stage roots for every pass
+    std::vector<double2> host;
+    size_t off_tw[MAX_PASSES] = {0}, off_wf[MAX_PASSES] = {0};
+    for (int i = 0; i < d.P - 1; ++i) {
+        off_tw[i] = host.size();
+        const std::vector<int> perm = stage_perm(d.F[i]);
+        for (int pp = 0; pp < d.F[i]; ++pp)
+            for (int r = 0; r < d.S[i]; ++r)
+                host.push_back(root_of_unity((uint64_t)r * (uint64_t)perm[pp], (uint64_t)d.Mi[i]));
+    }
+    for (int i = 0; i < d.P; ++i) {
+        off_wf[i] = host.size();
+        for (int e = 0; e < d.F[i]; ++e) host.push_back(root_of_unity((uint64_t)e, (uint64_t)d.F[i]));
+    }
+    if (cudaMalloc(&p->mem, host.size() * sizeof(double2)) != cudaSuccess) {
+        delete p;
+        return PG_ENOMEM;
+    }
+    if (cudaMemcpy(p->mem, host.data(), host.size() * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(p->mem);
+        delete p;
+        return PG_ECUDA;
+    }
+    for (int i = 0; i < d.P - 1; ++i) d.tw[i] = p->mem + off_tw[i];
+    for (int i = 0; i < d.P; ++i) d.wF[i] = p->mem + off_wf[i];
+    // CTA shapes: "small" for few slots (more, smaller CTAs), "big" for batches
+    const int Fl = d.F[d.P - 1];
+    p->Ginner_small = (Fl == 16) ? 8 : (Fl == 32) ? 4 : 2;
+    p->Ginner_big = (Fl >= 128) ? 4 : 8;
+    p->Gmid_small = 2;
+    p->Gmid_big = 8;
+    g_plans[lg] = p;
+    *out = p;
+    return PG_OK;
+}
+
+// Per-(n, M) weight tables: wf = a_j theta^j, wi = conj(theta^j) / (M a_j).
+struct Weights {
+    double2* wf = nullptr;
+    double2* wi = nullptr;
+    int refs = 0;
+};
+static std::map<std::pair<unsigned, unsigned>, Weights*> g_weights;
+
+static int get_weights(unsigned n, unsigned M, Weights** out) {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    auto key = std::make_pair(n, M);
+    auto it = g_weights.find(key);
+    if (it != g_weights.end()) {
+        it->second->refs++;
+        *out = it->second;
+        return PG_OK;
+    }
+    std::vector<double2> hf(M), hi(M);
+    const long double PI_L = 3.141592653589793238462643383279502884L;
+    for (unsigned j = 0; j < M; ++j) {
+        const unsigned long long S = ((unsigned long long)j * n + M - 1) / M;
+        const unsigned long long num = S * M - (unsigned long long)j * n;  // a_j = 2^(num / M)
+        const long double a = exp2l((long double)num / (long double)M);
+        const long double ang = PI_L * (long double)j / (2.0L * (long double)M);
+        const long double c = cosl(ang), s = sinl(ang);
+        hf[j] = make_double2((double)(a * c), (double)(a * s));
+        const long double sc = 1.0L / ((long double)M * a);
+        hi[j] = make_double2((double)(c * sc), (double)(-s * sc));
+    }
+    Weights* w = new Weights();
+    if (cudaMalloc(&w->wf, M * sizeof(double2)) != cudaSuccess ||
+        cudaMalloc(&w->wi, M * sizeof(double2)) != cudaSuccess) {
+        cudaFree(w->wf);
+        delete w;
+        return PG_ENOMEM;
+    }
+    cudaMemcpy(w->wf, hf.data(), M * sizeof(double2), cudaMemcpyHostToDevice);
+    cudaMemcpy(w->wi, hi.data(), M * sizeof(double2), cudaMemcpyHostToDevice);
+    w->refs = 1;
+    g_weights[key] = w;
+    *out = w;
+    return PG_OK;
+}
+
+static void put_weights(unsigned n, unsigned M) {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    auto it = g_weights.find(std::make_pair(n, M));
+    if (it == g_weights.end()) return;
+    if (--it->second->refs == 0) {
+        cudaFree(it->second->wf);
+        cudaFree(it->second->wi);
+        delete it->second;
+        g_weights.erase(it);
+    }
+}
+
+// Largest bits per digit allowed at each length (roundoff stays well under 0.4).
+static double max_bits_per_digit(int lg) {
+    static const double t[] = {19.5, 19.5, 19.0, 19.0, 18.5, 18.5, 18.0, 18.0, 17.5, 17.0, 16.5};
+    return t[std::min(std::max(lg - kMinLg, 0), kMaxLg - kMinLg)];
+}
+
+static int pick_lg(uint64_t k, unsigned n) {
+    (void)k;
+    if ((double)n / (double)(1 << kMinLg) < kMinBitsPerDigit) return -1;
+    for (int lg = kMinLg; lg <= kMaxLg; ++lg) {
+        const double bpd = (double)n / (double)(1 << lg);
+        if (bpd <= max_bits_per_digit(lg)) return lg;
+    }
+    return -1;
+}
+
+// ---------------------------------------------------------------------------
+// Slot pool: S residues of one FFT length advancing in lockstep.
+
+struct Pool {
+    Plan* plan = nullptr;
+    int S = 0;
+    unsigned M = 0;
+    int* digits = nullptr;
+    long long* carries = nullptr;
+    double2* spec = nullptr;
+    SlotState* st = nullptr;
+    Slot* dslots = nullptr;
+    std::vector<Slot> hslots;
+    std::vector<unsigned> slot_n;  // n bound to each slot's weights (0 = none)
+    int* rb_digits = nullptr;
+    long long* rb_top = nullptr;
+    int* h_rb_digits = nullptr;
+    long long* h_rb_top = nullptr;
+    SlotState* h_st = nullptr;  // pinned mirror
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0;
+    bool big = false;
+};
+
+template <int F0>
+static void launch_first(dim3 g, cudaStream_t s, const Slot* sl, const PlanDev& pd) {
+    k_first<F0><<<g, 2 * F0, 0, s>>>(sl, pd);
+}
+template <int F0>
+static void launch_last(dim3 g, cudaStream_t s, const Slot* sl, const PlanDev& pd) {
+    k_last<F0><<<g, 2 * F0, 0, s>>>(sl, pd);
+}
+
+static int enqueue_step_part(Pool* p, int part);
+
+static int enqueue_step(Pool* p) {
+    const PlanDev& d = p->plan->dev;
+    int nl = 0;  // kernels launched by the template dispatch below
+    const int nruns_cta = d.S[0] / RUN;
+    const dim3 g0(nruns_cta, p->S);
+    switch (d.F[0]) {
+        case 16: launch_first<16>(g0, p->stream, p->dslots, d); break;
+        case 32: launch_first<32>(g0, p->stream, p->dslots, d); break;
+        case 64: launch_first<64>(g0, p->stream, p->dslots, d); break;
+        case 128: launch_first<128>(g0, p->stream, p->dslots, d); break;
+        default: return PG_EINVAL;
+    }
+    const int Gm = p->big ? p->plan->Gmid_big : p->plan->Gmid_small;
+    if (d.P == 3) {
+        const dim3 gm(d.M / (d.F[1] * Gm), p->S);
+#define PG_MID(FF, GG) \
+    if (d.F[1] == FF && Gm == GG && ++nl) k_mid_fwd<FF, GG><<<gm, FF * GG / 4, 0, p->stream>>>(p->dslots, d);
+        PG_MID(32, 2) PG_MID(32, 8) PG_MID(64, 2) PG_MID(64, 8)
+#undef PG_MID
+    }
+    const int Gi = p->big ? p->plan->Ginner_big : p->plan->Ginner_small;
+    const int Fl = d.F[d.P - 1];
+    const dim3 gi(d.M / (Fl * Gi), p->S);
+#define PG_INNER(FF, GG, LP) \
+    if (Fl == FF && Gi == GG && d.P - 1 == LP && ++nl) k_inner<FF, GG, LP><<<gi, FF * GG / 4, 0, p->stream>>>(p->dslots, d);
+    PG_INNER(16, 8, 1) PG_INNER(32, 4, 1) PG_INNER(32, 8, 1) PG_INNER(64, 2, 1) PG_INNER(64, 8, 1)
+    PG_INNER(128, 2, 1) PG_INNER(128, 4, 1)
+    PG_INNER(32, 4, 2) PG_INNER(32, 8, 2) PG_INNER(64, 2, 2) PG_INNER(64, 8, 2)
+#undef PG_INNER
+    if (d.P == 3) {
+        const dim3 gm(d.M / (d.F[1] * Gm), p->S);
+#define PG_MIDI(FF, GG) \
+    if (d.F[1] == FF && Gm == GG && ++nl) k_mid_inv<FF, GG><<<gm, FF * GG / 4, 0, p->stream>>>(p->dslots, d);
+        PG_MIDI(32, 2) PG_MIDI(32, 8) PG_MIDI(64, 2) PG_MIDI(64, 8)
+#undef PG_MIDI
+    }
+    if (nl != (d.P == 3 ? 3 : 1)) return PG_EINVAL;  // no kernel instance for this shape
+    switch (d.F[0]) {
+        case 16: launch_last<16>(g0, p->stream, p->dslots, d); break;
+        case 32: launch_last<32>(g0, p->stream, p->dslots, d); break;
+        case 64: launch_last<64>(g0, p->stream, p->dslots, d); break;
+        case 128: launch_last<128>(g0, p->stream, p->dslots, d); break;
+    }
+    PG_CK(cudaGetLastError());
+    return PG_OK;
+}
+
+// Launch one kernel of the step sequence: part 0 = first pass, then mid fwd,
+// inner, mid inv (three-pass plans), last pass.  Returns PG_EINVAL past the end.
+static int enqueue_step_part(Pool* p, int part) {
+    const PlanDev& d = p->plan->dev;
+    const int parts = d.P == 3 ? 5 : 3;
+    if (part < 0 || part >= parts) return PG_EINVAL;
+    // reuse the full sequence launcher by masking: simplest is a dedicated switch
+    const dim3 g0(d.S[0] / RUN, p->S);
+    const int Gm = p->big ? p->plan->Gmid_big : p->plan->Gmid_small;
+    const int Gi = p->big ? p->plan->Ginner_big : p->plan->Ginner_small;
+    const int Fl = d.F[d.P - 1];
+    int nl = 0;
+    if (part == 0) {
+        switch (d.F[0]) {
+            case 16: launch_first<16>(g0, p->stream, p->dslots, d); break;
+            case 32: launch_first<32>(g0, p->stream, p->dslots, d); break;
+            case 64: launch_first<64>(g0, p->stream, p->dslots, d); break;
+            case 128: launch_first<128>(g0, p->stream, p->dslots, d); break;
+        }
+    } else if (part == parts - 1) {
+        switch (d.F[0]) {
+            case 16: launch_last<16>(g0, p->stream, p->dslots, d); break;
+            case 32: launch_last<32>(g0, p->stream, p->dslots, d); break;
+            case 64: launch_last<64>(g0, p->stream, p->dslots, d); break;
+            case 128: launch_last<128>(g0, p->stream, p->dslots, d); break;
+        }
+    } else if ((d.P == 3 && part == 2) || (d.P == 2 && part == 1)) {
+        const dim3 gi(d.M / (Fl * Gi), p->S);
+#define PG_INNER2(FF, GG, LP) \
+    if (Fl == FF && Gi == GG && d.P - 1 == LP && ++nl) k_inner<FF, GG, LP><<<gi, FF * GG / 4, 0, p->stream>>>(p->dslots, d);
+        PG_INNER2(16, 8, 1) PG_INNER2(32, 4, 1) PG_INNER2(32, 8, 1) PG_INNER2(64, 2, 1) PG_INNER2(64, 8, 1)
+        PG_INNER2(128, 2, 1) PG_INNER2(128, 4, 1)
+        PG_INNER2(32, 4, 2) PG_INNER2(32, 8, 2) PG_INNER2(64, 2, 2) PG_INNER2(64, 8, 2)
+#undef PG_INNER2
+    } else {
+        const dim3 gm(d.M / (d.F[1] * Gm), p->S);
+#define PG_MID2(FF, GG)                                                                      \
+    if (d.F[1] == FF && Gm == GG && ++nl) {                                                 \
+        if (part == 1) k_mid_fwd<FF, GG><<<gm, FF * GG / 4, 0, p->stream>>>(p->dslots, d);  \
+        else k_mid_inv<FF, GG><<<gm, FF * GG / 4, 0, p->stream>>>(p->dslots, d);            \
+    }
+        PG_MID2(32, 2) PG_MID2(32, 8) PG_MID2(64, 2) PG_MID2(64, 8)
+#undef PG_MID2
+    }
+    PG_CK(cudaGetLastError());
+    return PG_OK;
+}
+
+static void pool_free(Pool* p) {
+    if (!p) return;
+    if (p->graph) cudaGraphExecDestroy(p->graph);
+    for (int s = 0; s < p->S; ++s)
+        if (p->slot_n[s]) put_weights(p->slot_n[s], p->M);
+    cudaFree(p->digits);
+    cudaFree(p->carries);
+    cudaFree(p->spec);
+    cudaFree(p->st);
+    cudaFree(p->dslots);
+    cudaFree(p->rb_digits);
+    cudaFree(p->rb_top);
+    cudaFreeHost(p->h_rb_digits);
+    cudaFreeHost(p->h_rb_top);
+    cudaFreeHost(p->h_st);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+static int pool_create(int lg, int S, Pool** out) {
+    Plan* plan = nullptr;
+    int rc = get_plan(lg, &plan);
+    if (rc) return rc;
+    Pool* p = new Pool();
+    p->plan = plan;
+    p->S = S;
+    p->M = 1u << lg;
+    p->big = (S > 4);
+    p->hslots.resize(S);
+    p->slot_n.assign(S, 0);
+    const size_t M = p->M, nruns = M / RUN;
+    bool ok = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaMalloc(&p->digits, S * M * sizeof(int)) == cudaSuccess &&
+              cudaMalloc(&p->carries, S * nruns * 2 * sizeof(long long)) == cudaSuccess &&
+              cudaMalloc(&p->spec, S * M * sizeof(double2)) == cudaSuccess &&
+              cudaMalloc(&p->st, S * sizeof(SlotState)) == cudaSuccess &&
+              cudaMalloc(&p->dslots, S * sizeof(Slot)) == cudaSuccess &&
+              cudaMalloc(&p->rb_digits, S * M * sizeof(int)) == cudaSuccess &&
+              cudaMalloc(&p->rb_top, S * sizeof(long long)) == cudaSuccess &&
+              cudaMallocHost(&p->h_rb_digits, S * M * sizeof(int)) == cudaSuccess &&
+              cudaMallocHost(&p->h_rb_top, S * sizeof(long long)) == cudaSuccess &&
+              cudaMallocHost(&p->h_st, S * sizeof(SlotState)) == cudaSuccess;
+    if (!ok) {
+        pool_free(p);
+        return PG_ENOMEM;
+    }
+    cudaMemset(p->digits, 0, S * M * sizeof(int));
+    cudaMemset(p->carries, 0, S * nruns * 2 * sizeof(long long));
+    cudaMemset(p->st, 0, S * sizeof(SlotState));
+    memset(p->h_st, 0, S * sizeof(SlotState));
+    for (int s = 0; s < S; ++s) {
+        Slot& sl = p->hslots[s];
+        memset(&sl, 0, sizeof(sl));
+        sl.digits = p->digits + (size_t)s * M;
+        sl.carries = p->carries + (size_t)s * nruns * 2;
+        sl.spec = p->spec + (size_t)s * M;
+        sl.st = p->st + s;
+    }
+    if (cudaMemcpy(p->dslots, p->hslots.data(), S * sizeof(Slot), cudaMemcpyHostToDevice) != cudaSuccess) {
+        pool_free(p);
+        return PG_ECUDA;
+    }
+    *out = p;
+    return PG_OK;
+}
+
+// Bind slot s to candidate (k, n): weights and descriptor (host-synchronous).
+static int pool_bind(Pool* p, int s, uint64_t k, unsigned n) {
+    if (p->slot_n[s] != n) {
+        if (p->slot_n[s]) put_weights(p->slot_n[s], p->M);
+        p->slot_n[s] = 0;
+        Weights* w = nullptr;
+        int rc = get_weights(n, p->M, &w);
+        if (rc) return rc;
+        p->slot_n[s] = n;
+        p->hslots[s].wf = w->wf;
+        p->hslots[s].wi = w->wi;
+    }
+    p->hslots[s].k = k;
+    p->hslots[s].n = n;
+    PG_CK(cudaMemcpyAsync(p->dslots + s, &p->hslots[s], sizeof(Slot), cudaMemcpyHostToDevice, p->stream));
+    return PG_OK;
+}
+
+// Load canonical x into slot s: y = x 2^n mod N, digits + pending top.
+static int pool_load(Pool* p, int s, const Limbs& x, uint64_t k, unsigned n, const SlotState& st0) {
+    const unsigned M = p->M;
+    const Limbs y = to_mont(mod_N(x, k, n), k, n);
+    int* hd = p->h_rb_digits + (size_t)s * M;
+    long long top = 0;
+    value_to_digits(y, M, n, hd, &top);
+    const size_t nruns = M / RUN;
+    std::vector<long long> car(nruns * 2, 0);
+    car[2 * (nruns - 1)] = top;                 // pending top enters as the last run's carry
+    car[2 * (nruns - 1) + 1] = top < 0 ? -1 : 0;
+    PG_CK(cudaMemcpyAsync(p->hslots[s].digits, hd, M * sizeof(int), cudaMemcpyHostToDevice, p->stream));
+    PG_CK(cudaMemcpyAsync(p->hslots[s].carries, car.data(), car.size() * sizeof(long long),
+                          cudaMemcpyHostToDevice, p->stream));
+    p->h_st[s] = st0;
+    p->h_st[s].top = 0;
+    PG_CK(cudaMemcpyAsync(p->st + s, &p->h_st[s], sizeof(SlotState), cudaMemcpyHostToDevice, p->stream));
+    PG_CK(cudaStreamSynchronize(p->stream));  // car is a host temporary
+    return PG_OK;
+}
+
+// Canonical x of every slot (resolves pending carries on the device).
+static int pool_readback(Pool* p) {
+    const PlanDev& d = p->plan->dev;
+    const int nruns = d.M / RUN;
+    const dim3 g((nruns + 127) / 128, p->S);
+    k_readback<<<g, 128, 0, p->stream>>>(p->dslots, d, p->rb_digits, p->rb_top);
+    PG_CK(cudaGetLastError());
+    PG_CK(cudaMemcpyAsync(p->h_rb_digits, p->rb_digits, (size_t)p->S * d.M * sizeof(int), cudaMemcpyDeviceToHost,
+                          p->stream));
+    PG_CK(cudaMemcpyAsync(p->h_rb_top, p->rb_top, p->S * sizeof(long long), cudaMemcpyDeviceToHost, p->stream));
+    PG_CK(cudaMemcpyAsync(p->h_st, p->st, p->S * sizeof(SlotState), cudaMemcpyDeviceToHost, p->stream));
+    PG_CK(cudaStreamSynchronize(p->stream));
+    return PG_OK;
+}
+
+static Limbs slot_value(Pool* p, int s) {
+    const Slot& sl = p->hslots[s];
+    const Limbs y = digits_to_value(p->h_rb_digits + (size_t)s * p->M, p->M, sl.n, p->h_rb_top[s], sl.k);
+    return from_mont(y, sl.k, sl.n);
+}
+
+// Run `steps` kernel-sequence steps on the pool stream (graph replay when possible).
+static int pool_run(Pool* p, long long steps, bool use_graph) {
+    const int GSTEPS = 50;
+    if (use_graph && steps >= GSTEPS && !p->graph) {
+        cudaGraph_t g;
+        PG_CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = PG_OK;
+        for (int i = 0; i < GSTEPS && rc == PG_OK; ++i) rc = enqueue_step(p);
+        cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
+        if (rc) return rc;
+        PG_CK(ce);
+        PG_CK(cudaGraphInstantiate(&p->graph, g, 0));
+        cudaGraphDestroy(g);
+        p->graph_steps = GSTEPS;
+    }
+    while (steps > 0) {
+        if (use_graph && p->graph && steps >= p->graph_steps) {
+            PG_CK(cudaGraphLaunch(p->graph, p->stream));
+            steps -= p->graph_steps;
+        } else {
+            int rc = enqueue_step(p);
+            if (rc) return rc;
+            steps -= 1;
+        }
+    }
+    return PG_OK;
+}
+
+static double bits_to_double(unsigned long long b) {
+    double d;
+    memcpy(&d, &b, sizeof(d));
+    return d;
+}
+
+}  // namespace pg
+
+using namespace pg;
+
+// ---------------------------------------------------------------------------
+// single-candidate engine
+
+struct pg_engine {
+    uint64_t k = 0;
+    unsigned n = 0;
+    unsigned flags = 0;
+    int lg = 0;
+    Pool* pool = nullptr;
+    // rollback snapshot (device) of the slot
+    int* snap_digits = nullptr;
+    long long* snap_carries = nullptr;
+    SlotState* snap_st = nullptr;
+    double max_err = 0.0;
+    uint64_t squarings = 0;
+    uint32_t checks = 0, failures = 0, bumps = 0;
+    uint32_t gerbicz_block = 1000, gerbicz_every = 0;
+    bool loaded = false;
+};
+
+static int engine_alloc(pg_engine* e, int lg) {
+    Pool* p = nullptr;
+    int rc = pool_create(lg, 1, &p);
+    if (rc) return rc;
+    rc = pool_bind(p, 0, e->k, e->n);
+    if (rc) {
+        pool_free(p);
+        return rc;
+    }
+    const size_t M = p->M, nruns = M / RUN;
+    cudaFree(e->snap_digits);
+    cudaFree(e->snap_carries);
+    cudaFree(e->snap_st);
+    e->snap_digits = nullptr;
+    e->snap_carries = nullptr;
+    e->snap_st = nullptr;
+    if (cudaMalloc(&e->snap_digits, M * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&e->snap_carries, nruns * 2 * sizeof(long long)) != cudaSuccess ||
+        cudaMalloc(&e->snap_st, sizeof(SlotState)) != cudaSuccess) {
+        pool_free(p);
+        return PG_ENOMEM;
+    }
+    if (e->pool) pool_free(e->pool);
+    e->pool = p;
+    e->lg = lg;
+    return PG_OK;
+}
+
+static int snapshot(pg_engine* e, bool restore) {
+    Pool* p = e->pool;
+    const size_t M = p->M, nruns = M / RUN;
+    const Slot& sl = p->hslots[0];
+    if (!restore) {
+        PG_CK(cudaMemcpyAsync(e->snap_digits, sl.digits, M * sizeof(int), cudaMemcpyDeviceToDevice, p->stream));
+        PG_CK(cudaMemcpyAsync(e->snap_carries, sl.carries, nruns * 2 * sizeof(long long), cudaMemcpyDeviceToDevice,
+                              p->stream));
+        PG_CK(cudaMemcpyAsync(e->snap_st, sl.st, sizeof(SlotState), cudaMemcpyDeviceToDevice, p->stream));
+    } else {
+        PG_CK(cudaMemcpyAsync(sl.digits, e->snap_digits, M * sizeof(int), cudaMemcpyDeviceToDevice, p->stream));
+        PG_CK(cudaMemcpyAsync(sl.carries, e->snap_carries, nruns * 2 * sizeof(long long), cudaMemcpyDeviceToDevice,
+                              p->stream));
+        PG_CK(cudaMemcpyAsync(sl.st, e->snap_st, sizeof(SlotState), cudaMemcpyDeviceToDevice, p->stream));
+    }
+    return PG_OK;
+}
+
+static int read_state(pg_engine* e, SlotState* out) {
+    Pool* p = e->pool;
+    PG_CK(cudaMemcpyAsync(p->h_st, p->st, sizeof(SlotState), cudaMemcpyDeviceToHost, p->stream));
+    PG_CK(cudaStreamSynchronize(p->stream));
+    *out = p->h_st[0];
+    return PG_OK;
+}
+
+static int write_state(pg_engine* e, const SlotState& s) {
+    Pool* p = e->pool;
+    p->h_st[0] = s;
+    PG_CK(cudaMemcpyAsync(p->st, p->h_st, sizeof(SlotState), cudaMemcpyHostToDevice, p->stream));
+    return PG_OK;
+}
+
+// Move the current residue to a larger FFT length (after roundoff > 0.4).
+static int engine_bump(pg_engine* e) {
+    if (e->lg >= kMaxLg || (e->flags & PG_FLAG_NO_BUMP)) return PG_EROUNDOFF;
+    if ((double)e->n / (double)(2u << e->lg) < kMinBitsPerDigit) return PG_EROUNDOFF;
+    int rc = pool_readback(e->pool);
+    if (rc) return rc;
+    const Limbs x = slot_value(e->pool, 0);
+    SlotState st = e->pool->h_st[0];
+    rc = engine_alloc(e, e->lg + 1);
+    if (rc) return rc;
+    st.maxerr_bits = 0;
+    st.flags = 0;
+    rc = pool_load(e->pool, 0, x, e->k, e->n, st);
+    if (rc) return rc;
+    e->bumps++;
+    return PG_OK;
+}
+
+// Advance `steps` schedule steps with roundoff monitoring, chunk-wise rollback and bumps.
+static int engine_advance(pg_engine* e, uint64_t steps) {
+    const uint64_t CHUNK = 2000;
+    int guard = 0;
+    while (steps > 0) {
+        const uint64_t c = std::min<uint64_t>(steps, CHUNK);
+        SlotState st;
+        int rc = read_state(e, &st);
+        if (rc) return rc;
+        rc = snapshot(e, false);
+        if (rc) return rc;
+        st.total = st.step + (long long)c;
+        st.maxerr_bits = 0;
+        rc = write_state(e, st);
+        if (rc) return rc;
+        rc = pool_run(e->pool, (long long)c, !(e->flags & PG_FLAG_NO_GRAPH));
+        if (rc) return rc;
+        SlotState after;
+        rc = read_state(e, &after);
+        if (rc) return rc;
+        const double err = bits_to_double(after.maxerr_bits);
+        if (err > 0.4 || after.flags != 0 || after.step != st.total) {
+            // roll back this chunk and retry at the next FFT length
+            rc = snapshot(e, true);
+            if (rc) return rc;
+            PG_CK(cudaStreamSynchronize(e->pool->stream));
+            rc = engine_bump(e);
+            if (rc) return rc;
+            if (++guard > 8) return PG_EROUNDOFF;
+            continue;
+        }
+        e->max_err = std::max(e->max_err, err);
+        e->squarings += c;
+        steps -= c;
+    }
+    return PG_OK;
+}
+
+extern "C" {
+
+const char* pg_strerror(int s) {
+    switch (s) {
+        case PG_OK: return "ok";
+        case PG_EINVAL: return "invalid argument";
+        case PG_ENOMEM: return "out of memory";
+        case PG_EROUNDOFF: return "roundoff above 0.4 at the largest FFT length";
+        case PG_EGERBICZ: return "Gerbicz check failed";
+        case PG_ETIMEOUT: return "bounded wait expired";
+        case PG_ECUDA: return g_last_error[0] ? g_last_error : "CUDA error";
+        case PG_EIO: return "checkpoint I/O error";
+        case PG_ENODEV: return "no sm_103 device";
+        case PG_ESTATE: return "handle not ready";
+        case PG_EOVERFLOW: return "digit overflow";
+        default: return "unknown status";
+    }
+}
+
+int pg_version(void) { return 100; }
+
+int pg_device_info(char* name, size_t name_len, int* sm_count) {
+    cudaDeviceProp prop;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return PG_ENODEV;
+    if (name && name_len) snprintf(name, name_len, "%s", prop.name);
+    if (sm_count) *sm_count = prop.multiProcessorCount;
+    if (prop.major != 10 || prop.minor != 3) return PG_ENODEV;
+    return PG_OK;
+}
+
+uint32_t pg_pick_fft_len(uint64_t k, uint32_t n) {
+    const int lg = pick_lg(k, n);
+    return lg < 0 ? 0u : (1u << lg);
+}
+
+int pg_gate_rejects(uint64_t k, uint32_t n) { return gate_rejects(k, n) ? 1 : 0; }
+
+uint64_t pg_choose_base(uint64_t k, uint32_t n) { return choose_base(k, n); }
+
+int pg_host_roundtrip(uint64_t k, uint32_t n, uint32_t M, const uint64_t* x, size_t n_limbs, uint64_t* out,
+                      size_t out_limbs) {
+    if (!x || !out || M < 16 || (M & (M - 1)) || k == 0 || n < 2) return PG_EINVAL;
+    const Limbs xv(x, x + n_limbs);
+    const Limbs y = to_mont(mod_N(xv, k, n), k, n);
+    std::vector<int32_t> d(M);
+    long long top = 0;
+    value_to_digits(y, M, n, d.data(), &top);
+    const Limbs back = from_mont(digits_to_value(d.data(), M, n, top, k), k, n);
+    if (back.size() > out_limbs) return PG_EINVAL;
+    memset(out, 0, out_limbs * sizeof(uint64_t));
+    std::copy(back.begin(), back.end(), out);
+    return PG_OK;
+}
+
+int pg_create(uint64_t k, uint32_t n, uint32_t fft_len_hint, uint32_t flags, pg_engine** out) {
+    if (!out || k == 0 || (k & 1) == 0 || n < 2 || k >= (1ull << 40)) return PG_EINVAL;
+    *out = nullptr;
+    int lg = pick_lg(k, n);
+    if (fft_len_hint) {
+        int h = 0;
+        while ((1u << h) < fft_len_hint) ++h;
+        lg = (flags & PG_FLAG_FORCE_LEN) ? h : std::max(lg, h);
+    }
+    if (lg >= kMinLg && (double)n / (double)(1 << lg) < kMinBitsPerDigit) return PG_EINVAL;
+    if (lg < 0 || lg > kMaxLg) return PG_EINVAL;
+    lg = std::max(lg, kMinLg);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PG_ENODEV;
+    pg_engine* e = new pg_engine();
+    e->k = k;
+    e->n = n;
+    e->flags = flags;
+    int rc = engine_alloc(e, lg);
+    if (rc) {
+        delete e;
+        return rc;
+    }
+    *out = e;
+    return PG_OK;
+}
+
+int pg_destroy(pg_engine* e) {
+    if (!e) return PG_EINVAL;
+    if (e->pool) cudaStreamSynchronize(e->pool->stream);
+    pool_free(e->pool);
+    cudaFree(e->snap_digits);
+    cudaFree(e->snap_carries);
+    cudaFree(e->snap_st);
+    delete e;
+    return PG_OK;
+}
+
+int pg_set_residue(pg_engine* e, const uint64_t* limbs, size_t n_limbs) {
+    if (!e || (!limbs && n_limbs)) return PG_EINVAL;
+    Limbs x(limbs, limbs + n_limbs);
+    SlotState st;
+    memset(&st, 0, sizeof(st));
+    st.mul = 1;
+    int rc = pool_load(e->pool, 0, x, e->k, e->n, st);
+    if (rc) return rc;
+    e->loaded = true;
+    return PG_OK;
+}
+
+int pg_get_residue(pg_engine* e, uint64_t* limbs, size_t n_limbs) {
+    if (!e || !limbs) return PG_EINVAL;
+    if (!e->loaded) return PG_ESTATE;
+    int rc = pool_readback(e->pool);
+    if (rc) return rc;
+    const Limbs x = slot_value(e->pool, 0);
+    if (x.size() > n_limbs) return PG_EINVAL;
+    memset(limbs, 0, n_limbs * sizeof(uint64_t));
+    std::copy(x.begin(), x.end(), limbs);
+    return PG_OK;
+}
+
+int pg_square(pg_engine* e, uint64_t iters) {
+    if (!e) return PG_EINVAL;
+    if (!e->loaded) return PG_ESTATE;
+    return engine_advance(e, iters);
+}
+
+int pg_pow_small(pg_engine* e, uint64_t base_a, uint64_t exponent) {
+    if (!e || base_a == 0 || base_a > 0x7fffffff) return PG_EINVAL;
+    if (exponent == 0) {
+        const uint64_t one = 1;
+        return pg_set_residue(e, &one, 1);
+    }
+    const uint64_t a = base_a;
+    int rc = pg_set_residue(e, &a, 1);
+    if (rc) return rc;
+    SlotState st;
+    rc = read_state(e, &st);
+    if (rc) return rc;
+    st.kexp = exponent;
+    st.kbits = (int)bitlen(exponent);
+    st.mul = (int)base_a;
+    rc = write_state(e, st);
+    if (rc) return rc;
+    const uint64_t before = e->squarings;
+    rc = engine_advance(e, (uint64_t)st.kbits - 1);
+    e->squarings = before;  // the powering steps are not squarings of the test loop
+    return rc;
+}
+
+int pg_max_err(pg_engine* e, double* out, int reset) {
+    if (!e || !out) return PG_EINVAL;
+    *out = e->max_err;
+    if (reset) e->max_err = 0.0;
+    return PG_OK;
+}
+
+int pg_fft_len(const pg_engine* e, uint32_t* out) {
+    if (!e || !out) return PG_EINVAL;
+    *out = e->pool->M;
+    return PG_OK;
+}
+
+int pg_set_gerbicz(pg_engine* e, uint32_t block, uint32_t verify_every_blocks) {
+    if (!e || block == 0) return PG_EINVAL;
+    e->gerbicz_block = block;
+    e->gerbicz_every = verify_every_blocks;
+    return PG_OK;
+}
+
+int pg_stats(const pg_engine* e, uint64_t* squarings, uint32_t* checks, uint32_t* failures, uint32_t* bumps) {
+    if (!e) return PG_EINVAL;
+    if (squarings) *squarings = e->squarings;
+    if (checks) *checks = e->checks;
+    if (failures) *failures = e->failures;
+    if (bumps) *bumps = e->bumps;
+    return PG_OK;
+}
+
+int pg_time_squarings(pg_engine* e, uint64_t iters, double* ms, uint32_t* kernels_per_step) {
+    if (!e || !ms) return PG_EINVAL;
+    if (!e->loaded) return PG_ESTATE;
+    SlotState st;
+    int rc = read_state(e, &st);
+    if (rc) return rc;
+    st.total = st.step + (long long)iters;
+    rc = write_state(e, st);
+    if (rc) return rc;
+    cudaEvent_t a, b;
+    PG_CK(cudaEventCreate(&a));
+    PG_CK(cudaEventCreate(&b));
+    PG_CK(cudaEventRecord(a, e->pool->stream));
+    rc = pool_run(e->pool, (long long)iters, !(e->flags & PG_FLAG_NO_GRAPH));
+    PG_CK(cudaEventRecord(b, e->pool->stream));
+    PG_CK(cudaEventSynchronize(b));
+    float f = 0.f;
+    cudaEventElapsedTime(&f, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = f;
+    if (kernels_per_step) *kernels_per_step = e->pool->plan->dev.P == 3 ? 5 : 3;
+    if (!rc) e->squarings += iters;
+    return rc;
+}
+
+int pg_profile_step(pg_engine* e, double* times, uint32_t cap, uint32_t* count) {
+    if (!e || !times || !count) return PG_EINVAL;
+    if (!e->loaded) return PG_ESTATE;
+    SlotState st;
+    int rc = read_state(e, &st);
+    if (rc) return rc;
+    st.total = st.step + 1;
+    rc = write_state(e, st);
+    if (rc) return rc;
+    const int parts = e->pool->plan->dev.P == 3 ? 5 : 3;
+    std::vector<cudaEvent_t> ev(parts + 1);
+    for (auto& x : ev) PG_CK(cudaEventCreate(&x));
+    PG_CK(cudaEventRecord(ev[0], e->pool->stream));
+    for (int i = 0; i < parts && rc == PG_OK; ++i) {
+        rc = enqueue_step_part(e->pool, i);
+        cudaEventRecord(ev[i + 1], e->pool->stream);
+    }
+    PG_CK(cudaEventSynchronize(ev[parts]));
+    *count = 0;
+    for (int i = 0; i < parts && (uint32_t)i < cap; ++i) {
+        float f = 0.f;
+        cudaEventElapsedTime(&f, ev[i], ev[i + 1]);
+        times[i] = f;
+        *count = i + 1;
+    }
+    for (auto& x : ev) cudaEventDestroy(x);
+    if (!rc) e->squarings += 1;
+    return rc;
+}
+
+int pg_debug_corrupt(pg_engine* e, uint32_t index, int32_t delta) {
+    if (!e || index >= e->pool->M) return PG_EINVAL;
+    k_corrupt<<<1, 32, 0, e->pool->stream>>>(e->pool->dslots, 0, index, delta);
+    PG_CK(cudaGetLastError());
+    PG_CK(cudaStreamSynchronize(e->pool->stream));
+    return PG_OK;
+}
+
+}  // extern "C"
+
+#include "pg_engine_more.inc"

@@ -1,0 +1,491 @@
+// pg_kernels.cuh -- sm_103a kernels of one modular squaring y <- s * y^2 * 2^-n mod N.
+//
+// One squaring of a residue with M digits is a length-M complex FFT pair in
+// "right-angle" form: digit j enters as d_j * a_j * theta^j (a_j: IBDWT weight
+// 2^{S_j - jn/M}, theta = e^{i pi / 2M}), so the cyclic length-M transform
+// computes the negacyclic length-2M product of the real digit sequence.  The
+// digit sequence occupies only the low half, so nothing wraps: after the
+// inverse transform element j holds c_j + i c_{M+j}, the low and high halves
+// of the zero-padded product X^2.  The Montgomery fold (2^-n = -k mod N) then
+// needs only element j:  u_j = s (c_{M+j} + 2 top d_j - k c_j).
+//
+// The transform runs as P passes over a global buffer (radix F[0] x ... x
+// F[P-1] = M, decimation in frequency forward, in time inverse, no bit
+// reversal: the pointwise square does not care about order).  Kernels:
+//   k_first   pass 0 forward, fused with the carry fix-up of the previous
+//             squaring, the top-digit reduction, and the forward weight
+//   k_mid_*   pass 1 forward / inverse (P == 3 only)
+//   k_inner   last pass forward, pointwise square, last pass inverse
+//   k_last    pass 0 inverse, fused with unweight, rounding + max |err|,
+//             the Montgomery fold and the in-run carry
+// All arithmetic on the transform is FP64; rounding, fold and carries are
+// exact integer (int64 / int128) work.  Slots (candidates) run side by side:
+// blockIdx.y is the slot.
+#ifndef PG_KERNELS_CUH
+#define PG_KERNELS_CUH
+
+#include "pg_internal.h"
+
+namespace pg {
+
+typedef __int128 i128;
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 w) {
+    return make_double2(fma(a.x, w.x, -(a.y * w.y)), fma(a.x, w.y, a.y * w.x));
+}
+// a * conj(w)
+__device__ __forceinline__ double2 cmulc(double2 a, double2 w) {
+    return make_double2(fma(a.x, w.x, a.y * w.y), fma(a.y, w.x, -(a.x * w.y)));
+}
+
+// Radix-4 decimation-in-frequency butterfly, outputs in place (0,1,2,3).
+__device__ __forceinline__ void bfly4_fwd(double2& a0, double2& a1, double2& a2, double2& a3) {
+    const double apcx = a0.x + a2.x, apcy = a0.y + a2.y;
+    const double amcx = a0.x - a2.x, amcy = a0.y - a2.y;
+    const double bpdx = a1.x + a3.x, bpdy = a1.y + a3.y;
+    const double bmdx = a1.x - a3.x, bmdy = a1.y - a3.y;
+    a0 = make_double2(apcx + bpdx, apcy + bpdy);
+    a2 = make_double2(apcx - bpdx, apcy - bpdy);
+    a1 = make_double2(amcx + bmdy, amcy - bmdx);  // (a0-a2) - i (a1-a3)
+    a3 = make_double2(amcx - bmdy, amcy + bmdx);  // (a0-a2) + i (a1-a3)
+}
+// Inverse radix-4 butterfly (conjugate DFT, unscaled).
+__device__ __forceinline__ void bfly4_inv(double2& z0, double2& z1, double2& z2, double2& z3) {
+    const double sx = z0.x + z2.x, sy = z0.y + z2.y;
+    const double dx = z0.x - z2.x, dy = z0.y - z2.y;
+    const double tx = z1.x + z3.x, ty = z1.y + z3.y;
+    const double ux = z1.x - z3.x, uy = z1.y - z3.y;
+    z0 = make_double2(sx + tx, sy + ty);
+    z2 = make_double2(sx - tx, sy - ty);
+    z1 = make_double2(dx - uy, dy + ux);  // (z0-z2) + i (z1-z3)
+    z3 = make_double2(dx + uy, dy - ux);  // (z0-z2) - i (z1-z3)
+}
+
+template <int F>
+struct Lg { static constexpr int v = (F <= 1) ? 0 : 1 + Lg<F / 2>::v; };
+template <>
+struct Lg<1> { static constexpr int v = 0; };
+
+// Element (group g, index i) of a shared-memory tile.
+template <int F, int G, bool GROUP_MAJOR>
+__device__ __forceinline__ int tix(int g, int i) {
+    return GROUP_MAJOR ? g * F + i : i * G + g;
+}
+
+// In-place forward DFT of length F on G groups of a shared tile, NT threads.
+// Radix-4 stages with spans F/4, F/16, ...; a final radix-2 stage if log2 F is
+// odd.  Output order is the digit reversal that the host's permutation table
+// (plan construction) describes; the inverse below undoes it exactly.
+template <int F, int G, int NT, bool GM>
+__device__ __forceinline__ void smem_fft_fwd(double2* tile, const double2* __restrict__ wF) {
+    constexpr int LG = Lg<F>::v;
+    constexpr int N4 = LG / 2;
+#pragma unroll
+    for (int s = 0; s < N4; ++s) {
+        const int h = F >> (2 * (s + 1));
+        const int step = F / (4 * h);
+        for (int b = threadIdx.x; b < G * F / 4; b += NT) {
+            const int g = b / (F / 4), w = b % (F / 4);
+            const int blk = w / h, j = w % h;
+            const int i0 = blk * 4 * h + j;
+            double2 a0 = tile[tix<F, G, GM>(g, i0)];
+            double2 a1 = tile[tix<F, G, GM>(g, i0 + h)];
+            double2 a2 = tile[tix<F, G, GM>(g, i0 + 2 * h)];
+            double2 a3 = tile[tix<F, G, GM>(g, i0 + 3 * h)];
+            bfly4_fwd(a0, a1, a2, a3);
+            if (h > 1) {
+                const int e = j * step;
+                a1 = cmul(a1, wF[e]);
+                a2 = cmul(a2, wF[2 * e]);
+                a3 = cmul(a3, wF[3 * e]);
+            }
+            tile[tix<F, G, GM>(g, i0)] = a0;
+            tile[tix<F, G, GM>(g, i0 + h)] = a1;
+            tile[tix<F, G, GM>(g, i0 + 2 * h)] = a2;
+            tile[tix<F, G, GM>(g, i0 + 3 * h)] = a3;
+        }
+        __syncthreads();
+    }
+    if (LG & 1) {
+        for (int b = threadIdx.x; b < G * F / 2; b += NT) {
+            const int g = b / (F / 2), i0 = 2 * (b % (F / 2));
+            const double2 a = tile[tix<F, G, GM>(g, i0)];
+            const double2 c = tile[tix<F, G, GM>(g, i0 + 1)];
+            tile[tix<F, G, GM>(g, i0)] = make_double2(a.x + c.x, a.y + c.y);
+            tile[tix<F, G, GM>(g, i0 + 1)] = make_double2(a.x - c.x, a.y - c.y);
+        }
+        __syncthreads();
+    }
+}
+
+// Exact inverse (times F) of smem_fft_fwd.
+template <int F, int G, int NT, bool GM>
+__device__ __forceinline__ void smem_fft_inv(double2* tile, const double2* __restrict__ wF) {
+    constexpr int LG = Lg<F>::v;
+    constexpr int N4 = LG / 2;
+    if (LG & 1) {
+        for (int b = threadIdx.x; b < G * F / 2; b += NT) {
+            const int g = b / (F / 2), i0 = 2 * (b % (F / 2));
+            const double2 a = tile[tix<F, G, GM>(g, i0)];
+            const double2 c = tile[tix<F, G, GM>(g, i0 + 1)];
+            tile[tix<F, G, GM>(g, i0)] = make_double2(a.x + c.x, a.y + c.y);
+            tile[tix<F, G, GM>(g, i0 + 1)] = make_double2(a.x - c.x, a.y - c.y);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int s = N4 - 1; s >= 0; --s) {
+        const int h = F >> (2 * (s + 1));
+        const int step = F / (4 * h);
+        for (int b = threadIdx.x; b < G * F / 4; b += NT) {
+            const int g = b / (F / 4), w = b % (F / 4);
+            const int blk = w / h, j = w % h;
+            const int i0 = blk * 4 * h + j;
+            double2 z0 = tile[tix<F, G, GM>(g, i0)];
+            double2 z1 = tile[tix<F, G, GM>(g, i0 + h)];
+            double2 z2 = tile[tix<F, G, GM>(g, i0 + 2 * h)];
+            double2 z3 = tile[tix<F, G, GM>(g, i0 + 3 * h)];
+            if (h > 1) {
+                const int e = j * step;
+                z1 = cmulc(z1, wF[e]);
+                z2 = cmulc(z2, wF[2 * e]);
+                z3 = cmulc(z3, wF[3 * e]);
+            }
+            bfly4_inv(z0, z1, z2, z3);
+            tile[tix<F, G, GM>(g, i0)] = z0;
+            tile[tix<F, G, GM>(g, i0 + h)] = z1;
+            tile[tix<F, G, GM>(g, i0 + 2 * h)] = z2;
+            tile[tix<F, G, GM>(g, i0 + 3 * h)] = z3;
+        }
+        __syncthreads();
+    }
+}
+
+// ---- digit geometry and integer helpers ----
+
+// S_j = ceil(j n / M): bit position of digit j (S_M = n).
+__device__ __forceinline__ unsigned long long digit_pos(unsigned long long j, unsigned n, int lgM) {
+    return (j * n + ((1ull << lgM) - 1)) >> lgM;
+}
+__device__ __forceinline__ int digit_width(unsigned long long j, unsigned n, int lgM) {
+    return (int)(digit_pos(j + 1, n, lgM) - digit_pos(j, n, lgM));
+}
+
+__device__ __forceinline__ i128 load_carry(const long long* c, long long idx) {
+    const unsigned long long lo = (unsigned long long)c[2 * idx];
+    const long long hi = c[2 * idx + 1];
+    return (i128)(((unsigned __int128)(unsigned long long)hi << 64) | lo);
+}
+__device__ __forceinline__ void store_carry(long long* c, long long idx, i128 v) {
+    c[2 * idx] = (long long)(unsigned long long)v;
+    c[2 * idx + 1] = (long long)(v >> 64);
+}
+
+// Small multiplier of step i: the left-to-right binary powering x <- x^2 a^bit
+// over the bits of kexp below its top bit, then 1 (plain squaring).
+__device__ __forceinline__ int sched_mul(const SlotState* st, long long i) {
+    if (st->kexp == 0 || i < 0 || i >= (long long)st->kbits - 1) return 1;
+    return ((st->kexp >> (st->kbits - 2 - i)) & 1ull) ? st->mul : 1;
+}
+
+// Split v into a balanced digit of width b (returned) and the carry (left in v).
+__device__ __forceinline__ long long take_digit(i128& v, int b) {
+    long long lo = (long long)((unsigned long long)v & ((1ull << b) - 1));
+    if (lo >= (1ll << (b - 1))) lo -= (1ll << b);
+    v = (v - (i128)lo) >> b;
+    return lo;
+}
+
+__device__ __forceinline__ i128 floor_div(i128 a, i128 b) {  // b > 0
+    i128 q = a / b;
+    if ((a % b) != 0 && a < 0) q -= 1;
+    return q;
+}
+
+// Carry entering run `run` of a slot.  For run 0 it is minus the quotient of
+// the top-digit reduction: top' = s_prev top^2 + (carry out of the last run)
+// is split as q k + t with |t| <= k/2, and q k 2^n = -q (mod N).
+__device__ __forceinline__ i128 run_carry_in(const Slot& sl, long long run, long long nruns,
+                                             long long step, long long* new_top) {
+    if (run > 0) return load_carry(sl.carries, run - 1);
+    const SlotState* st = sl.st;
+    const i128 clast = load_carry(sl.carries, nruns - 1);
+    const long long top = st->top;
+    const int sp = (step > 0) ? sched_mul(st, step - 1) : 1;
+    const i128 tp = (i128)sp * (i128)top * (i128)top + clast;
+    const i128 kk = (i128)sl.k;
+    const i128 q = floor_div(2 * tp + kk, 2 * kk);
+    *new_top = (long long)(tp - q * kk);
+    return -q;
+}
+
+// Fold an incoming carry into the RUN digits of one run.  The carry shrinks
+// by a digit width per position; whatever is left at the last digit of the run
+// is added there unnormalised, so the run's own carry-out stays valid.
+__device__ __forceinline__ void fixup_run(int (&dv)[RUN], i128 c, unsigned long long j0, unsigned n,
+                                          int lgM, int& bad) {
+#pragma unroll
+    for (int t = 0; t < RUN; ++t) {
+        if (c != 0) {
+            i128 v = (i128)dv[t] + c;
+            if (t < RUN - 1) {
+                const int b = digit_width(j0 + t, n, lgM);
+                dv[t] = (int)take_digit(v, b);
+                c = v;
+            } else {
+                if (v > (i128)(1 << 30) || v < -(i128)(1 << 30)) bad = 1;
+                dv[t] = (int)v;
+                c = 0;
+            }
+        }
+    }
+}
+
+// Round x to the nearest integer (ties to even) with one FP64 add of 1.5*2^52;
+// tracks max |x - round(x)| as the bits of a non-negative double.
+__device__ __forceinline__ long long round_track(double x, unsigned long long& emax, int& bad) {
+    const double MAGIC = 6755399441055744.0;  // 1.5 * 2^52
+    const long long bits = __double_as_longlong(x);
+    if (((bits >> 52) & 0x7FF) >= 1023 + 50) bad = 1;  // |x| >= 2^50: outside the exact range
+    const double y = x + MAGIC;
+    const long long r = __double_as_longlong(y) - 0x4338000000000000LL;
+    const double e = fabs(x - (y - MAGIC));
+    const unsigned long long eb = (unsigned long long)__double_as_longlong(e);
+    emax = eb > emax ? eb : emax;
+    return r;
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// k_first: pass 0 forward.  CTA = RUN consecutive columns r (so each row of
+// the tile is one carry run) x F0 rows q; grid (S0 / RUN, slots).
+template <int F0>
+__global__ void __launch_bounds__(2 * F0) k_first(const Slot* __restrict__ slots, const PlanDev pl) {
+    constexpr int G = RUN, NT = 2 * F0;
+    __shared__ double2 tile[F0 * G];
+    __shared__ int dsm[F0 * G];
+    const Slot sl = slots[blockIdx.y];
+    SlotState* st = sl.st;
+    const long long step = st->step;
+    const bool act = step < st->total;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->active = act ? 1 : 0;
+    if (!act) return;
+    const int S0 = pl.S[0];
+    const int r0 = blockIdx.x * G;
+    const long long nruns = pl.M / RUN;
+    const int tid = threadIdx.x;
+    if (tid < F0) {
+        const unsigned long long j0 = (unsigned long long)r0 + (unsigned long long)tid * S0;
+        const long long run = (long long)(j0 / RUN);
+        int4* dp = reinterpret_cast<int4*>(sl.digits + j0);
+        const int4 v0 = dp[0], v1 = dp[1];
+        int dv[RUN] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+        long long new_top = 0;
+        const i128 cin = run_carry_in(sl, run, nruns, step, &new_top);
+        if (run == 0) st->top = new_top;
+        int bad = 0;
+        fixup_run(dv, cin, j0, sl.n, pl.lgM, bad);
+        if (bad) atomicOr(&st->flags, SF_DIGIT_OVERFLOW);
+        dp[0] = make_int4(dv[0], dv[1], dv[2], dv[3]);
+        dp[1] = make_int4(dv[4], dv[5], dv[6], dv[7]);
+#pragma unroll
+        for (int t = 0; t < RUN; ++t) dsm[tid * G + t] = dv[t];
+    }
+    __syncthreads();
+    for (int e = tid; e < F0 * G; e += NT) {
+        const int q = e / G, t = e % G;
+        const double2 w = sl.wf[r0 + t + q * S0];
+        const double d = (double)dsm[e];
+        tile[e] = make_double2(d * w.x, d * w.y);
+    }
+    __syncthreads();
+    smem_fft_fwd<F0, G, NT, false>(tile, pl.wF[0]);
+    const double2* __restrict__ tw = pl.tw[0];
+    for (int e = tid; e < F0 * G; e += NT) {
+        const int p = e / G, t = e % G;
+        const int r = r0 + t;
+        sl.spec[r + p * S0] = cmul(tile[e], tw[p * S0 + r]);
+    }
+}
+
+// k_mid_fwd / k_mid_inv: pass 1 of a three-pass plan.  CTA = G consecutive
+// columns of one block of length Mi[1]; grid (M / (F G), slots).
+template <int F, int G>
+__global__ void __launch_bounds__(F * G / 4) k_mid_fwd(const Slot* __restrict__ slots, const PlanDev pl) {
+    constexpr int NT = F * G / 4;
+    __shared__ double2 tile[F * G];
+    const Slot sl = slots[blockIdx.y];
+    if (!sl.st->active) return;
+    const int S = pl.S[1], Mi = pl.Mi[1];
+    const int cpb = S / G;
+    const int blk = blockIdx.x / cpb, r0 = (blockIdx.x % cpb) * G;
+    double2* base = sl.spec + (size_t)blk * Mi;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < F * G; e += NT) {
+        const int q = e / G, t = e % G;
+        tile[e] = base[r0 + t + q * S];
+    }
+    __syncthreads();
+    smem_fft_fwd<F, G, NT, false>(tile, pl.wF[1]);
+    const double2* __restrict__ tw = pl.tw[1];
+    for (int e = tid; e < F * G; e += NT) {
+        const int p = e / G, t = e % G;
+        const int r = r0 + t;
+        base[r + p * S] = cmul(tile[e], tw[p * S + r]);
+    }
+}
+
+template <int F, int G>
+__global__ void __launch_bounds__(F * G / 4) k_mid_inv(const Slot* __restrict__ slots, const PlanDev pl) {
+    constexpr int NT = F * G / 4;
+    __shared__ double2 tile[F * G];
+    const Slot sl = slots[blockIdx.y];
+    if (!sl.st->active) return;
+    const int S = pl.S[1], Mi = pl.Mi[1];
+    const int cpb = S / G;
+    const int blk = blockIdx.x / cpb, r0 = (blockIdx.x % cpb) * G;
+    double2* base = sl.spec + (size_t)blk * Mi;
+    const double2* __restrict__ tw = pl.tw[1];
+    const int tid = threadIdx.x;
+    for (int e = tid; e < F * G; e += NT) {
+        const int p = e / G, t = e % G;
+        const int r = r0 + t;
+        tile[e] = cmulc(base[r + p * S], tw[p * S + r]);
+    }
+    __syncthreads();
+    smem_fft_inv<F, G, NT, false>(tile, pl.wF[1]);
+    for (int e = tid; e < F * G; e += NT) {
+        const int q = e / G, t = e % G;
+        base[r0 + t + q * S] = tile[e];
+    }
+}
+
+// k_inner: last pass.  CTA = G contiguous groups of F; forward, square, inverse.
+template <int F, int G, int LASTP>
+__global__ void __launch_bounds__(F * G / 4) k_inner(const Slot* __restrict__ slots, const PlanDev pl) {
+    constexpr int NT = F * G / 4;
+    __shared__ double2 tile[F * G];
+    const Slot sl = slots[blockIdx.y];
+    SlotState* st = sl.st;
+    if (!st->active) return;
+    const int tid = threadIdx.x;
+    if (blockIdx.x == 0 && tid == 0) st->step += 1;  // nobody reads step until k_last
+    double2* base = sl.spec + (size_t)blockIdx.x * (F * G);
+    for (int e = tid; e < F * G; e += NT) tile[e] = base[e];
+    __syncthreads();
+    smem_fft_fwd<F, G, NT, true>(tile, pl.wF[LASTP]);
+    for (int e = tid; e < F * G; e += NT) {
+        const double2 z = tile[e];
+        tile[e] = make_double2(fma(z.x, z.x, -(z.y * z.y)), (z.x + z.x) * z.y);
+    }
+    __syncthreads();
+    smem_fft_inv<F, G, NT, true>(tile, pl.wF[LASTP]);
+    for (int e = tid; e < F * G; e += NT) base[e] = tile[e];
+}
+
+// k_last: pass 0 inverse + unweight + round + fold + carry within each run.
+template <int F0>
+__global__ void __launch_bounds__(2 * F0) k_last(const Slot* __restrict__ slots, const PlanDev pl) {
+    constexpr int G = RUN, NT = 2 * F0;
+    __shared__ double2 tile[F0 * G];
+    __shared__ long long cl[F0 * G];
+    __shared__ long long ch[F0 * G];
+    __shared__ unsigned long long wmax[NT / 32];
+    const Slot sl = slots[blockIdx.y];
+    SlotState* st = sl.st;
+    if (!st->active) return;
+    const int S0 = pl.S[0];
+    const int r0 = blockIdx.x * G;
+    const int tid = threadIdx.x;
+    const double2* __restrict__ tw = pl.tw[0];
+    for (int e = tid; e < F0 * G; e += NT) {
+        const int p = e / G, t = e % G;
+        const int r = r0 + t;
+        tile[e] = cmulc(sl.spec[r + p * S0], tw[p * S0 + r]);
+    }
+    __syncthreads();
+    smem_fft_inv<F0, G, NT, false>(tile, pl.wF[0]);
+    unsigned long long emax = 0;
+    int badr = 0;
+    for (int e = tid; e < F0 * G; e += NT) {
+        const int q = e / G, t = e % G;
+        const double2 z = cmul(tile[e], sl.wi[r0 + t + q * S0]);
+        cl[e] = round_track(z.x, emax, badr);
+        ch[e] = round_track(z.y, emax, badr);
+    }
+    if (badr) {
+        emax = (unsigned long long)__double_as_longlong(1.0);
+        atomicOr(&st->flags, SF_ROUND_RANGE);
+    }
+    emax = warp_max_u64(emax);
+    if ((tid & 31) == 0) wmax[tid >> 5] = emax;
+    __syncthreads();
+    if (tid == 0) {
+        unsigned long long m = 0;
+        for (int w = 0; w < NT / 32; ++w) m = wmax[w] > m ? wmax[w] : m;
+        atomicMax(&st->maxerr_bits, m);
+    }
+    if (tid < F0) {
+        const unsigned long long j0 = (unsigned long long)r0 + (unsigned long long)tid * S0;
+        const long long run = (long long)(j0 / RUN);
+        int4* dp = reinterpret_cast<int4*>(sl.digits + j0);
+        const int4 v0 = dp[0], v1 = dp[1];
+        const int dv[RUN] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+        const i128 top2 = 2 * (i128)st->top;
+        const i128 s = (i128)sched_mul(st, st->step - 1);
+        const i128 kk = (i128)sl.k;
+        i128 carry = 0;
+        int nd[RUN];
+#pragma unroll
+        for (int t = 0; t < RUN; ++t) {
+            const int e = tid * G + t;
+            const i128 u = s * ((i128)ch[e] + top2 * (i128)dv[t] - kk * (i128)cl[e]);
+            carry += u;
+            nd[t] = (int)take_digit(carry, digit_width(j0 + t, sl.n, pl.lgM));
+        }
+        dp[0] = make_int4(nd[0], nd[1], nd[2], nd[3]);
+        dp[1] = make_int4(nd[4], nd[5], nd[6], nd[7]);
+        store_carry(sl.carries, run, carry);
+    }
+}
+
+// k_readback: resolve the pending carries of each slot into out_digits /
+// out_top without changing the slot state.  One thread per run.
+__global__ void k_readback(const Slot* __restrict__ slots, const PlanDev pl, int* __restrict__ out_digits,
+                           long long* __restrict__ out_top) {
+    const Slot sl = slots[blockIdx.y];
+    const long long nruns = pl.M / RUN;
+    const long long run = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (run >= nruns) return;
+    const unsigned long long j0 = (unsigned long long)run * RUN;
+    const int* dp = sl.digits + j0;
+    int dv[RUN];
+#pragma unroll
+    for (int t = 0; t < RUN; ++t) dv[t] = dp[t];
+    long long new_top = 0;
+    const i128 cin = run_carry_in(sl, run, nruns, sl.st->step, &new_top);
+    int bad = 0;
+    fixup_run(dv, cin, j0, sl.n, pl.lgM, bad);
+    int* op = out_digits + (size_t)blockIdx.y * pl.M + j0;
+#pragma unroll
+    for (int t = 0; t < RUN; ++t) op[t] = dv[t];
+    if (run == 0) out_top[blockIdx.y] = new_top;
+    if (bad) atomicOr(&sl.st->flags, SF_DIGIT_OVERFLOW);
+}
+
+// Test hook: add delta to one pending digit (a simulated silent memory error).
+__global__ void k_corrupt(const Slot* __restrict__ slots, int slot, unsigned index, int delta) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) slots[slot].digits[index] += delta;
+}
+
+}  // namespace pg
+
+#endif

@@ -1,0 +1,182 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the reference's own
+golden vectors, GMP and the oracle.  Integer results must be bit-exact."""
+import json
+import os
+import random
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden.json")
+M64 = (1 << 64) - 1
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import prothlogic_gb300 as pgm
+    pgm.load()
+    return pgm
+
+
+@pytest.fixture(scope="module")
+def golden():
+    with open(GOLDEN) as f:
+        return json.load(f)
+
+
+def _N(k, n):
+    return k * (1 << n) + 1
+
+
+def test_device_is_gb300(pg):
+    import ctypes
+    name = ctypes.create_string_buffer(64)
+    sm = ctypes.c_int()
+    assert pg.load().pg_device_info(name, 64, ctypes.byref(sm)) == 0, name.value
+    assert sm.value >= 100
+
+
+@pytest.mark.parametrize("k,n", [(3, 2048), (843, 4096), (9999, 5000), (77, 8300), (524287, 20000),
+                                 (5, 32700), (12345, 65536), (999999, 131072), (3, 270000)])
+def test_steps_match_python(pg, k, n):
+    N = _N(k, n)
+    x = random.Random(n * 31 + k).randrange(N)
+    with pg.Engine(k, n, flags=pg.FLAG_NO_GRAPH) as e:
+        e.set_residue(x)
+        assert e.get_residue() == x
+        for i in range(10):
+            e.square(1)
+            x = x * x % N
+            assert e.get_residue() == x, f"step {i}"
+        assert e.max_err() < 0.4
+
+
+def test_reference_traces(pg, gmp, golden):
+    """RES64 after every squaring equals the reference engine's (corrected L)."""
+    for t in golden["traces"]:
+        k, n = t["k"], t["n"]
+        with pg.Engine(k, n) as e:
+            e.pow_small(t["a"], k)
+            if n <= 70000:
+                assert e.get_residue() == gmp.powmod(t["a"], k, _N(k, n))
+            for i, want in enumerate(t["res64"]):
+                e.square(1)
+                got = e.get_residue()
+                assert format(got & M64, "016x") == want, (k, n, i)
+
+
+def test_reference_full_tests(pg, golden):
+    for t in golden["tests"]:
+        r = pg.proth_test(t["k"], t["n"])
+        assert r["status"] == 0
+        assert r["verdict"] == t["verdict"], t
+        assert r["base"] == t["base"], t
+        assert format(r["res64"], "016x") == t["res64"], t
+
+
+def test_known_answers(pg, golden):
+    """843*2^120002+1 prime (a=5), 853 and 895 composite -- RES64 equal to the reference's."""
+    for t in golden["known"]:
+        r = pg.proth_test(t["k"], t["n"])
+        assert (r["verdict"], r["base"], format(r["res64"], "016x")) == (t["verdict"], t["base"], t["res64"])
+    assert pg.execute_proth_test_fft(843, 120002) is True
+
+
+def test_large_configuration_residues(pg, golden):
+    """n = 2^20: x0 = a, RES64 after every 1,000 of 10,000 squarings (GMP values)."""
+    g = golden["large"]
+    with pg.Engine(g["k"], g["n"]) as e:
+        assert e.fft_len == 65536
+        e.set_residue(g["a"])
+        for i, want in enumerate(g["res64"]):
+            e.square(g["every"])
+            assert format(e.get_residue() & M64, "016x") == want, i
+        assert e.max_err() < 0.4
+
+
+def test_gmp_full_tests_batched(pg, golden):
+    b = pg.Batch(16)
+    for i, t in enumerate(golden["gmp_tests"]):
+        b.submit(t["k"], t["n"], i)
+    b.run(0)
+    res = {r["tag"]: r for r in b.poll()}
+    assert len(res) == len(golden["gmp_tests"])
+    for i, t in enumerate(golden["gmp_tests"]):
+        r = res[i]
+        assert (r["verdict"], r["base"], format(r["res64"], "016x")) == (t["verdict"], t["base"], t["res64"]), t
+    b.close()
+
+
+def test_batch_equals_single(pg, oracle):
+    rng = random.Random(17)
+    cands = [(2 * rng.randrange(1, 5000) + 1, rng.randrange(2048, 9000)) for _ in range(60)]
+    b = pg.Batch(24)
+    for i, (k, n) in enumerate(cands):
+        b.submit(k, n, i)
+    b.run(0)
+    res = {r["tag"]: r for r in b.poll()}
+    assert len(res) == len(cands)
+    for i, (k, n) in enumerate(cands[:12]):
+        s = pg.proth_test(k, n)
+        assert (res[i]["verdict"], res[i]["res64"], res[i]["base"]) == (s["verdict"], s["res64"], s["base"])
+    for i, (k, n) in enumerate(cands):
+        o = oracle.proth_test(k, n)
+        assert (res[i]["verdict"], res[i]["res64"], res[i]["base"]) == (o["verdict"], o["res64"], o["base"]), (k, n)
+    b.close()
+
+
+def test_pow_small(pg):
+    for k, n, a in [(843, 4096, 5), (999999, 65536, 3), (3, 2500, 37)]:
+        N = _N(k, n)
+        with pg.Engine(k, n) as e:
+            e.pow_small(a, k)
+            assert e.get_residue() == pow(a, k, N)
+            e.pow_small(a, 1)
+            assert e.get_residue() == a
+
+
+def test_checkpoint_roundtrip(pg, tmp_path):
+    k, n = 9999, 32768
+    N = _N(k, n)
+    path = str(tmp_path / "check.bin")
+    with pg.Engine(k, n) as e:
+        e.set_residue(7)
+        e.square(500)
+        e.checkpoint_save(path, 499)
+        e.square(300)
+        want = e.get_residue()
+    assert want == pow(7, 1 << 800, N)
+    with open(path, "rb") as f:
+        raw = f.read()
+    import struct
+    ci, nl = struct.unpack("<QQ", raw[:16])
+    assert ci == 499 and nl >= (n + 64) // 64
+    x = int.from_bytes(raw[16:16 + 8 * nl], "little")
+    assert x == pow(7, 1 << 500, N)
+    with pg.Engine(k, n) as e2:
+        assert e2.checkpoint_load(path) == 499
+        e2.square(300)
+        assert e2.get_residue() == want
+
+
+def test_roundoff_bump_recovers(pg):
+    """A forced, far too small FFT length overflows the rounding range; the
+    engine rolls back, grows the length and still returns the exact residue."""
+    k, n = 999999, 65536
+    N = _N(k, n)
+    with pg.Engine(k, n, fft_len_hint=1024, flags=pg.FLAG_FORCE_LEN) as e:
+        assert e.fft_len == 1024
+        e.set_residue(5)
+        e.square(50)
+        assert e.get_residue() == pow(5, 1 << 50, N)
+        assert e.stats()["fft_bumps"] >= 1
+        assert e.fft_len > 1024
+
+
+def test_roundoff_without_bump_reports(pg):
+    with pg.Engine(999999, 65536, fft_len_hint=1024, flags=pg.FLAG_FORCE_LEN | pg.FLAG_NO_BUMP) as e:
+        e.set_residue(5)
+        with pytest.raises(pg.ProthGpuError) as ei:
+            e.square(20)
+        assert ei.value.status == pg.PG_EROUNDOFF

@@ -1,0 +1,88 @@
+"""Host-side checks that need no GPU: the C-ABI library loads and exports every
+symbol the header declares; host conversions and Proth-test decisions."""
+import os
+import random
+import re
+
+import pytest
+
+import prothlogic_gb300 as pg
+from prothlogic_gb300 import workloads
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    with open(os.path.join(ROOT, "include", "prothgpu.h")) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"\b(pg_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = pg.load()
+    names = _declared()
+    assert len(names) >= 25
+    for name in names:
+        assert hasattr(lib, name), name
+        assert name in pg.SIGNATURES, f"{name} missing from the Python binding"
+
+
+def test_version_and_strerror():
+    lib = pg.load()
+    assert lib.pg_version() >= 100
+    assert lib.pg_strerror(3).decode().startswith("roundoff")
+
+
+@pytest.mark.parametrize("k,n,M", [(3, 2048, 256), (843, 120002, 8192), (524287, 1048576, 65536),
+                                   (9999, 32768, 2048), (77, 8300, 1024), (999999, 65536, 4096)])
+def test_host_representation_roundtrip(k, n, M):
+    N = k * (1 << n) + 1
+    rng = random.Random(n + k)
+    for x in [0, 1, N - 1, N - 2, rng.randrange(N), rng.randrange(N), (1 << n) - 1, k << n]:
+        assert pg.host_roundtrip(k, n, M, x) == x % N
+    # values above N are reduced
+    big = rng.randrange(N * N)
+    assert pg.host_roundtrip(k, n, M, big) == big % N
+
+
+def test_gate_and_base_match_oracle(oracle, gmp):
+    rng = random.Random(3)
+    L = oracle.lib()
+    for _ in range(200):
+        k = 2 * rng.randrange(1, 500000) + 1
+        n = rng.randrange(2048, 300000)
+        assert pg.gate_rejects(k, n) == bool(L.ora_gate_rejects(k, n))
+        assert pg.choose_base(k, n) == L.ora_choose_base(k, n)
+    assert pg.choose_base(843, 120002) == 5
+
+
+def test_fft_length_choice():
+    prev = 0
+    for n in [2048, 4096, 8192, 32768, 65536, 131072, 262144, 524288, 1 << 20]:
+        L = pg.pick_fft_len(3, n)
+        assert L >= prev and L & (L - 1) == 0
+        assert n / L <= 19.5
+        prev = L
+    assert pg.pick_fft_len(3, 1 << 20) == 65536
+    assert pg.pick_fft_len(3, 65536) == 4096
+    assert pg.pick_fft_len(3, 100) == 0  # below the smallest supported residue
+
+
+def test_workloads_are_seeded():
+    assert workloads.single(3) == workloads.single(3)
+    k, n = workloads.large()
+    assert n == 1 << 20 and k % 2 == 1 and 3 <= k < (1 << 20)
+    u = workloads.uniform(50)
+    assert all(n == 65536 and k % 2 == 1 and 3 <= k < 10 ** 6 for k, n in u)
+    v = workloads.uneven(200)
+    assert all(8192 <= n <= 262144 and k % 2 == 1 and k < 10 ** 5 for k, n in v)
+    s = workloads.serving(20, rate=10.0)
+    assert all(s[i][0] < s[i + 1][0] for i in range(19))
+
+
+def test_engine_fails_loudly_without_device():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(pg.ProthGpuError):
+        pg.Engine(3, 4096)
