@@ -1,0 +1,356 @@
+#!/usr/bin/env python3
+"""Headline benchmark: ns per modular squaring of one Proth candidate k*2^n+1
+with n = 1,048,576 (k odd, uniform in [3, 2^20) from seed 2, x0 = a), with a
+Gerbicz check over blocks of 1,000 squarings.
+
+One "step" is one Gerbicz block of 1,000 squarings.  The default run times
+K = 10 steps (10,000 squarings) after W = 3 warm-up steps; the Gerbicz
+verification of all K blocks runs inside the last timed step.
+
+  value  device time (CUDA events on the engine's stream) per squaring, residue
+         resident on the device, L2 flushed between steps;
+  e2e    the same metric through the public C ABI with host buffers: every step
+         uploads its input residue (pg_set_residue, H2D), squares 1,000 times
+         and returns a verified result (pg_get_residue, D2H);
+  --impl reference  the reference algorithm on this host's cores (the C oracle
+         restatement of prothlogic4.2's engine; the reference's AVX-512 code
+         itself only builds on x86-64), same metric and config.
+
+Multi-GPU: candidates do not shard, so N > 1 runs N independent replicas
+(one process per GPU) and `value` is the whole-job time per squaring.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from prothlogic_gb300 import workloads  # noqa: E402
+
+METRIC = "ns per mod-squaring (n=1,048,576)"
+UNIT = "ns/squaring"
+SQ_PER_STEP = 1000
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dp_ops_per_point(plan_F):
+    """FP64 instructions per complex point of one squaring, counted from the kernels."""
+    def fft(F):
+        lg = int(math.log2(F))
+        n4 = lg // 2
+        ops = 7 * (n4 - 1) + 4  # radix-4 stages with twiddles (7/pt) and the twiddle-free last one (4/pt)
+        if lg & 1:
+            ops = 7 * n4 + 2    # all radix-4 stages keep twiddles, then a radix-2 stage (2/pt)
+        return ops
+    F = plan_F
+    if len(F) == 3:
+        first = 2 + fft(F[0]) + 4
+        mid = fft(F[1]) + 4
+        inner = 2 * fft(F[2]) + 4
+        last = 4 + fft(F[0]) + 4 + 6
+        return first + 2 * mid + inner + last
+    first = 2 + fft(F[0]) + 4
+    inner = 2 * fft(F[1]) + 4
+    last = 4 + fft(F[0]) + 4 + 6
+    return first + inner + last
+
+
+PLAN_F = {256: (16, 16), 512: (16, 32), 1024: (32, 32), 2048: (32, 64), 4096: (64, 64), 8192: (64, 128),
+          16384: (128, 128), 32768: (32, 32, 32), 65536: (16, 64, 64), 131072: (32, 64, 64),
+          262144: (64, 64, 64)}
+
+
+def profile_traffic(kernel_regex_name):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "k_last_n1048576.txt")
+    try:
+        with open(path) as f:
+            for ln in f:
+                if ln.startswith("dram_bytes_per_launch:"):
+                    return float(ln.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pgd = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pgd = dist
+    return world, rank, local, pgd
+
+
+def barrier(pgd):
+    if pgd is not None:
+        pgd.barrier()
+
+
+def max_over_ranks(pgd, v):
+    if pgd is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pgd.all_reduce(t, op=pgd.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample_seconds():
+    return float(os.environ.get("PROTH_CPU_SAMPLE_S", "15"))
+
+
+def time_cpu_reference(k, n, a, budget_s, min_sq=4):
+    """Squarings of the reference algorithm on one host core (oracle/_ref on x86-64, else the C oracle port)."""
+    from oracle.build_oracle import build_ref
+    from tests import _oracle
+    L = _oracle.lib().ora_choose_L(n, k)
+    ref = build_ref() if os.environ.get("PROTH_USE_REF", "1") == "1" else None
+    if ref:
+        # engine-only microseconds per squaring of the unmodified reference engine
+        steps = max(min_sq, int(budget_s / 0.013))
+        out = subprocess.run([ref, "time", str(k), str(n), str(L), str(steps)], capture_output=True, text=True,
+                             check=True, cwd="/tmp")
+        us = float(out.stdout.strip().splitlines()[-1])
+        return us * 1e3, "reference", steps, L
+    ctx = _oracle.Ctx(L)
+    x = _oracle.to_limbs(a, L // 4)
+    t0 = time.perf_counter()
+    done = 0
+    while done < min_sq or time.perf_counter() - t0 < budget_s:
+        _oracle.lib().ora_run_squarings(ctx.h, x, n, k, 1)
+        done += 1
+    dt = time.perf_counter() - t0
+    return dt / done * 1e9, "port", done, L
+
+
+def run_reference(args, world, rank, pgd):
+    if rank != 0:
+        return 0
+    k, n = workloads.large()
+    import prothlogic_gb300 as pg
+    a = pg.choose_base(k, n)
+    per_step_budget = max(0.2, cpu_sample_seconds() / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        time_cpu_reference(k, n, a, per_step_budget, min_sq=2)
+    vals = []
+    kind, used, L = "port", 0, 0
+    for _ in range(args.steps):
+        ns, kind, used, L = time_cpu_reference(k, n, a, per_step_budget, min_sq=2)
+        vals.append(ns)
+    v = statistics.mean(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * SQ_PER_STEP / 1e6,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded candidate, no dataset)",
+            "config": {"workload": "large: n=1048576, k odd in [3,2^20) seed 2, x0=a", "k": k, "n": n,
+                       "fft_len_L": L, "squarings_per_step": SQ_PER_STEP},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": kind,
+                             "sample": f"{used} squarings per step at n=1048576, L={L}, one thread "
+                                       "(the reference's per-candidate engine is single-threaded)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, world, rank, local, pgd):
+    import prothlogic_gb300 as pg
+    pg.set_device(local)
+    k, n = workloads.large()
+    a = pg.choose_base(k, n)
+    K, W = args.steps, args.warmup
+    peaks = measured_peaks()
+    fp64_tflops = pg.measure_fp64_peak()
+
+    eng = pg.Engine(k, n)
+    M = eng.fft_len
+    # warm-up: W blocks, each verified
+    eng.set_gerbicz(SQ_PER_STEP, 0)
+    eng.set_residue(a)
+    for _ in range(W):
+        eng.square(SQ_PER_STEP)
+
+    # timed: K blocks of 1,000 squarings, verification of all K blocks in the last step
+    eng.set_gerbicz(SQ_PER_STEP, K)
+    eng.set_residue(a)
+    pg.flush_l2()
+    sampler = ClockSampler(local)
+    launches0 = pg.launch_count()
+    barrier(pgd)
+    sampler.start()
+    step_ms = []
+    for _ in range(K):
+        step_ms.append(eng.square_timed(SQ_PER_STEP))
+        pg.flush_l2()  # untimed, between steps
+    clocks = sampler.stop()
+    launches = pg.launch_count() - launches0 - K  # minus the flush memsets (not counted anyway)
+    total_ms = max_over_ranks(pgd, sum(step_ms))
+    stats = eng.stats()
+    res = eng.get_residue()
+    value = total_ms * 1e6 / (K * SQ_PER_STEP * world)
+
+    # parity of the timed run: RES64 after K*1000 squarings of x0 = a (GMP values)
+    parity = "unchecked"
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+            g = json.load(f)["large"]
+        if g["k"] == k and K * SQ_PER_STEP <= len(g["res64"]) * g["every"]:
+            want = g["res64"][K * SQ_PER_STEP // g["every"] - 1]
+            parity = "ok" if format(res & ((1 << 64) - 1), "016x") == want else "MISMATCH"
+    except (OSError, KeyError, IndexError):
+        pass
+
+    # e2e through the public API with host buffers, one verified block per step
+    eng.set_gerbicz(SQ_PER_STEP, 0)
+    x = a
+    barrier(pgd)
+    t0 = time.perf_counter()
+    for _ in range(K):
+        eng.set_residue(x)
+        eng.square(SQ_PER_STEP)
+        x = eng.get_residue()
+    e2e_s = max_over_ranks(pgd, time.perf_counter() - t0)
+    e2e = e2e_s * 1e9 / (K * SQ_PER_STEP * world)
+    nl_in = (x.bit_length() + 63) // 64
+    h2d = M * 4 + (M // 8) * 16 + 112          # digits, run carries, slot state
+    d2h = M * 4 + 8 + 112                       # canonical digits, top digit, slot state
+
+    # roofline: algorithmic bytes 32*E per squaring, E = ceil(W/8), W = n + bitlen(k)
+    Wbits = n + k.bit_length()
+    E = math.ceil(Wbits / 8)
+    t_sq = value * 1e-9 * world
+    bytes_alg = 32 * E
+    hbm_peak = peaks.get("hbm_gbs")
+    achieved_gbs = bytes_alg / t_sq / 1e9
+    dp_ops = dp_ops_per_point(PLAN_F[M]) * M
+    dp_rate = dp_ops / t_sq / 1e12                 # T instr/s
+    dp_peak = fp64_tflops / 2.0                    # DFMA instr/s from the live probe
+    traffic = profile_traffic("k_last")
+
+    if rank != 0:
+        eng.close()
+        return 0
+    cpu_ns, cpu_kind, cpu_used, cpu_L = time_cpu_reference(k, n, a, cpu_sample_seconds())
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": total_ms / K, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded candidate, no dataset)",
+        "config": {"workload": "large: n=1048576, k odd in [3,2^20) seed 2, x0=a, Gerbicz block 1000",
+                   "k": k, "n": n, "base_a": a, "fft_len": M, "squarings_per_step": SQ_PER_STEP,
+                   "gerbicz": f"block {SQ_PER_STEP}, {K} blocks verified in the last step",
+                   "l2": "flushed between steps (512 MiB write)", "parity_res64": parity,
+                   "gerbicz_checks": stats["gerbicz_checks"], "gerbicz_failures": stats["gerbicz_failures"],
+                   "fft_bumps": stats["fft_bumps"], "max_err": eng.max_err()},
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved_gbs / hbm_peak if hbm_peak else None, "traffic": traffic,
+                     "note": "measured hbm_gbs peak; per squaring (the 5 kernels of one squaring); "
+                             "the real bound is the FP64 pipe, see roofline_fp64"},
+        "roofline_fp64": {"bound": "fp64", "achieved": dp_rate, "peak": dp_peak, "unit": "T DP instr/s",
+                          "frac": dp_rate / dp_peak, "dp_instr_per_squaring": dp_ops,
+                          "peak_source": "live DFMA probe (pg_measure_fp64_peak), of measured",
+                          "flops_alg_per_squaring": 5 * E * math.log2(E),
+                          "achieved_alg_tflops": 5 * E * math.log2(E) / t_sq / 1e12,
+                          "fp64_peak_tflops": fp64_tflops},
+        "cpu_baseline": {"value": cpu_ns, "unit": UNIT, "cores": 1, "kind": cpu_kind,
+                         "sample": f"{cpu_used} squarings at n=1048576, L={cpu_L}, one host thread"},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "note": "set_residue + 1,000 squarings + verified get_residue per step"},
+        "clocks": clocks,
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+    eng.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local, pgd = dist_setup()
+    if args.impl == "reference":
+        rc = run_reference(args, world, rank, pgd)
+    else:
+        rc = run_gpu(args, world, rank, local, pgd)
+    if pgd is not None:
+        pgd.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

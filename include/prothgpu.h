@@ -113,6 +113,19 @@ int pg_time_squarings(pg_engine* e, uint64_t iters, double* ms, uint32_t* kernel
 /* Per-kernel device times (ms) of one squaring, launched one by one with an
  * event pair around each: times[i] for i < *count (at most cap). */
 int pg_profile_step(pg_engine* e, double* times, uint32_t cap, uint32_t* count);
+/* pg_square bracketed by CUDA events on the engine's stream: *ms is the device
+ * time of the whole call (squarings, Gerbicz products and checks, and the
+ * idle gaps of its host synchronisation). */
+int pg_square_timed(pg_engine* e, uint64_t iters, double* ms);
+/* Overwrite a device buffer larger than the L2 cache (between timed steps). */
+int pg_flush_l2(void);
+/* Kernels this library has launched so far (graph replays included). */
+uint64_t pg_launch_count(void);
+/* Select the CUDA device for the calling host thread (one process per GPU). */
+int pg_set_device(int device);
+/* Measured FP64 FMA throughput of this device (TFLOP/s, 2 flops per DFMA):
+ * a DFMA-only kernel, 4 x SM-count CTAs of 256 threads, 8 independent chains. */
+int pg_measure_fp64_peak(double* tflops);
 /* Test hook: add `delta` to residue digit `index` on the device (simulates a
  * silent memory error; nothing faults).  Used by the failure-detection tests. */
 int pg_debug_corrupt(pg_engine* e, uint32_t index, int32_t delta);

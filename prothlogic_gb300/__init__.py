@@ -71,6 +71,11 @@ SIGNATURES = {
     "pg_stats": (ctypes.c_int, [_vp, ctypes.POINTER(_u64), ctypes.POINTER(_u32), ctypes.POINTER(_u32),
                                 ctypes.POINTER(_u32)]),
     "pg_debug_corrupt": (ctypes.c_int, [_vp, _u32, _i32]),
+    "pg_measure_fp64_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
+    "pg_square_timed": (ctypes.c_int, [_vp, _u64, ctypes.POINTER(ctypes.c_double)]),
+    "pg_flush_l2": (ctypes.c_int, []),
+    "pg_launch_count": (_u64, []),
+    "pg_set_device": (ctypes.c_int, [ctypes.c_int]),
     "pg_time_squarings": (ctypes.c_int, [_vp, _u64, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_u32)]),
     "pg_profile_step": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), _u32, ctypes.POINTER(_u32)]),
     "pg_checkpoint_save": (ctypes.c_int, [_vp, ctypes.c_char_p, _u64]),
@@ -108,17 +113,30 @@ def _check(rc, what):
 
 
 def _to_limbs(x, nl):
-    arr = (_u64 * nl)()
-    for i in range(nl):
-        arr[i] = (x >> (64 * i)) & 0xFFFFFFFFFFFFFFFF
-    return arr
+    return (_u64 * nl).from_buffer_copy(int(x).to_bytes(8 * nl, "little"))
 
 
 def _from_limbs(arr):
-    v = 0
-    for i in reversed(range(len(arr))):
-        v = (v << 64) | int(arr[i])
-    return v
+    return int.from_bytes(bytes(arr), "little")
+
+
+def measure_fp64_peak():
+    """Measured DFMA throughput of the current GPU in TFLOP/s."""
+    v = ctypes.c_double()
+    _check(load().pg_measure_fp64_peak(ctypes.byref(v)), "pg_measure_fp64_peak")
+    return v.value
+
+
+def flush_l2():
+    _check(load().pg_flush_l2(), "pg_flush_l2")
+
+
+def launch_count():
+    return int(load().pg_launch_count())
+
+
+def set_device(device):
+    _check(load().pg_set_device(device), "pg_set_device")
 
 
 def pick_fft_len(k, n):
@@ -203,6 +221,12 @@ class Engine:
                "pg_stats")
         return {"squarings": sq.value, "gerbicz_checks": c.value, "gerbicz_failures": f.value,
                 "fft_bumps": b.value}
+
+    def square_timed(self, iters):
+        """pg_square with CUDA events on the engine stream around it; returns ms."""
+        ms = ctypes.c_double()
+        _check(load().pg_square_timed(self._h, iters, ctypes.byref(ms)), "pg_square_timed")
+        return ms.value
 
     def time_squarings(self, iters):
         """Device-timed squarings (CUDA events on the engine stream): (ms, kernels per squaring)."""

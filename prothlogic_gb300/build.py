@@ -24,10 +24,28 @@ def nvcc():
     return "nvcc"
 
 
+COMPAT_LIB = os.path.join(OUT_DIR, "libprothgpu_compat.a")
+COMPAT_DRIVER = os.path.join(OUT_DIR, "compat_driver")
+
+
+def build_compat():
+    """The reference-API shim (fft_init / fft_square_karatsuba / fft_destroy) and its test driver."""
+    comp = os.path.join(HERE, "compat")
+    obj = os.path.join(OUT_DIR, "fft_engine_gpu.o")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-fPIC", "-c", os.path.join(comp, "fft_engine_gpu.cpp"),
+                           "-o", obj])
+    subprocess.check_call(["ar", "rcs", COMPAT_LIB, obj])
+    subprocess.check_call(["g++", "-std=c++17", "-O2", os.path.join(comp, "compat_driver.cpp"), COMPAT_LIB,
+                           "-L" + OUT_DIR, "-lprothgpu", "-Wl,-rpath," + OUT_DIR, "-o", COMPAT_DRIVER])
+    return COMPAT_DRIVER
+
+
 def needs_build():
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
+    if not os.path.exists(COMPAT_DRIVER):
+        return True
     return any(os.path.getmtime(os.path.join(CSRC, d)) > t for d in DEPS)
 
 
@@ -56,6 +74,7 @@ def build(force=False, verbose=False):
     link = [nvcc(), "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
     subprocess.check_call(link)
     os.replace(tmp, LIB)
+    build_compat()
     return LIB
 
 

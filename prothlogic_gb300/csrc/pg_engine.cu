@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -35,6 +36,7 @@ namespace pg {
     } while (0)
 
 static thread_local char g_last_error[256];
+static std::atomic<unsigned long long> g_launches{0};  // kernels launched (graph replays included)
 static void note_cuda_error(cudaError_t e, const char* what, int line) {
     snprintf(g_last_error, sizeof(g_last_error), "%s (line %d): %s", what, line, cudaGetErrorString(e));
 }
@@ -49,7 +51,8 @@ struct Plan {
 };
 
 static const int kMinLg = 8, kMaxLg = 18;
-static const double kMinBitsPerDigit = 6.0;  // below this the run carries do not settle
+static const double kMinBitsPerDigit = 6.0;   // below this the run carries do not settle
+static const double kMaxBitsPerDigit = 24.0;  // balanced digits stay within int32 with room for carries
 
 static bool plan_radices(int lg, int F[MAX_PASSES], int& P) {
     switch (lg) {
@@ -247,120 +250,86 @@ struct Pool {
     long long* h_rb_top = nullptr;
     SlotState* h_st = nullptr;  // pinned mirror
     cudaStream_t stream = nullptr;
-    cudaGraphExec_t graph = nullptr;
-    int graph_steps = 0;
+    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (base, count) -> GSTEPS-step graph
     bool big = false;
+    bool capturing = false;
 };
 
+static const int GSTEPS = 50;  // steps per captured graph
+
 template <int F0>
-static void launch_first(dim3 g, cudaStream_t s, const Slot* sl, const PlanDev& pd) {
-    k_first<F0><<<g, 2 * F0, 0, s>>>(sl, pd);
+static void launch_first(dim3 g, cudaStream_t s, const Slot* sl, int base, const PlanDev& pd) {
+    k_first<F0><<<g, 2 * F0, 0, s>>>(sl, base, pd);
 }
 template <int F0>
-static void launch_last(dim3 g, cudaStream_t s, const Slot* sl, const PlanDev& pd) {
-    k_last<F0><<<g, 2 * F0, 0, s>>>(sl, pd);
+static void launch_last(dim3 g, cudaStream_t s, const Slot* sl, int base, const PlanDev& pd) {
+    k_last<F0><<<g, 2 * F0, 0, s>>>(sl, base, pd);
 }
 
-static int enqueue_step_part(Pool* p, int part);
+static int enqueue_step_part(Pool* p, int part, int base, int count);
 
-static int enqueue_step(Pool* p) {
-    const PlanDev& d = p->plan->dev;
-    int nl = 0;  // kernels launched by the template dispatch below
-    const int nruns_cta = d.S[0] / RUN;
-    const dim3 g0(nruns_cta, p->S);
-    switch (d.F[0]) {
-        case 16: launch_first<16>(g0, p->stream, p->dslots, d); break;
-        case 32: launch_first<32>(g0, p->stream, p->dslots, d); break;
-        case 64: launch_first<64>(g0, p->stream, p->dslots, d); break;
-        case 128: launch_first<128>(g0, p->stream, p->dslots, d); break;
-        default: return PG_EINVAL;
+static int enqueue_step(Pool* p, int base, int count) {
+    const int parts = p->plan->dev.P == 3 ? 5 : 3;
+    for (int i = 0; i < parts; ++i) {
+        const int rc = enqueue_step_part(p, i, base, count);
+        if (rc) return rc;
     }
-    const int Gm = p->big ? p->plan->Gmid_big : p->plan->Gmid_small;
-    if (d.P == 3) {
-        const dim3 gm(d.M / (d.F[1] * Gm), p->S);
-#define PG_MID(FF, GG) \
-    if (d.F[1] == FF && Gm == GG && ++nl) k_mid_fwd<FF, GG><<<gm, FF * GG / 4, 0, p->stream>>>(p->dslots, d);
-        PG_MID(32, 2) PG_MID(32, 8) PG_MID(64, 2) PG_MID(64, 8)
-#undef PG_MID
-    }
-    const int Gi = p->big ? p->plan->Ginner_big : p->plan->Ginner_small;
-    const int Fl = d.F[d.P - 1];
-    const dim3 gi(d.M / (Fl * Gi), p->S);
-#define PG_INNER(FF, GG, LP) \
-    if (Fl == FF && Gi == GG && d.P - 1 == LP && ++nl) k_inner<FF, GG, LP><<<gi, FF * GG / 4, 0, p->stream>>>(p->dslots, d);
-    PG_INNER(16, 8, 1) PG_INNER(32, 4, 1) PG_INNER(32, 8, 1) PG_INNER(64, 2, 1) PG_INNER(64, 8, 1)
-    PG_INNER(128, 2, 1) PG_INNER(128, 4, 1)
-    PG_INNER(32, 4, 2) PG_INNER(32, 8, 2) PG_INNER(64, 2, 2) PG_INNER(64, 8, 2)
-#undef PG_INNER
-    if (d.P == 3) {
-        const dim3 gm(d.M / (d.F[1] * Gm), p->S);
-#define PG_MIDI(FF, GG) \
-    if (d.F[1] == FF && Gm == GG && ++nl) k_mid_inv<FF, GG><<<gm, FF * GG / 4, 0, p->stream>>>(p->dslots, d);
-        PG_MIDI(32, 2) PG_MIDI(32, 8) PG_MIDI(64, 2) PG_MIDI(64, 8)
-#undef PG_MIDI
-    }
-    if (nl != (d.P == 3 ? 3 : 1)) return PG_EINVAL;  // no kernel instance for this shape
-    switch (d.F[0]) {
-        case 16: launch_last<16>(g0, p->stream, p->dslots, d); break;
-        case 32: launch_last<32>(g0, p->stream, p->dslots, d); break;
-        case 64: launch_last<64>(g0, p->stream, p->dslots, d); break;
-        case 128: launch_last<128>(g0, p->stream, p->dslots, d); break;
-    }
-    PG_CK(cudaGetLastError());
     return PG_OK;
 }
 
 // Launch one kernel of the step sequence: part 0 = first pass, then mid fwd,
 // inner, mid inv (three-pass plans), last pass.  Returns PG_EINVAL past the end.
-static int enqueue_step_part(Pool* p, int part) {
+static int enqueue_step_part(Pool* p, int part, int base, int count) {
     const PlanDev& d = p->plan->dev;
     const int parts = d.P == 3 ? 5 : 3;
-    if (part < 0 || part >= parts) return PG_EINVAL;
-    // reuse the full sequence launcher by masking: simplest is a dedicated switch
-    const dim3 g0(d.S[0] / RUN, p->S);
+    if (part < 0 || part >= parts || base < 0 || count < 1 || base + count > p->S) return PG_EINVAL;
+    const dim3 g0(d.S[0] / RUN, count);
     const int Gm = p->big ? p->plan->Gmid_big : p->plan->Gmid_small;
     const int Gi = p->big ? p->plan->Ginner_big : p->plan->Ginner_small;
     const int Fl = d.F[d.P - 1];
     int nl = 0;
     if (part == 0) {
         switch (d.F[0]) {
-            case 16: launch_first<16>(g0, p->stream, p->dslots, d); break;
-            case 32: launch_first<32>(g0, p->stream, p->dslots, d); break;
-            case 64: launch_first<64>(g0, p->stream, p->dslots, d); break;
-            case 128: launch_first<128>(g0, p->stream, p->dslots, d); break;
+            case 16: launch_first<16>(g0, p->stream, p->dslots, base, d); break;
+            case 32: launch_first<32>(g0, p->stream, p->dslots, base, d); break;
+            case 64: launch_first<64>(g0, p->stream, p->dslots, base, d); break;
+            case 128: launch_first<128>(g0, p->stream, p->dslots, base, d); break;
         }
     } else if (part == parts - 1) {
         switch (d.F[0]) {
-            case 16: launch_last<16>(g0, p->stream, p->dslots, d); break;
-            case 32: launch_last<32>(g0, p->stream, p->dslots, d); break;
-            case 64: launch_last<64>(g0, p->stream, p->dslots, d); break;
-            case 128: launch_last<128>(g0, p->stream, p->dslots, d); break;
+            case 16: launch_last<16>(g0, p->stream, p->dslots, base, d); break;
+            case 32: launch_last<32>(g0, p->stream, p->dslots, base, d); break;
+            case 64: launch_last<64>(g0, p->stream, p->dslots, base, d); break;
+            case 128: launch_last<128>(g0, p->stream, p->dslots, base, d); break;
         }
     } else if ((d.P == 3 && part == 2) || (d.P == 2 && part == 1)) {
-        const dim3 gi(d.M / (Fl * Gi), p->S);
+        const dim3 gi(d.M / (Fl * Gi), count);
 #define PG_INNER2(FF, GG, LP) \
-    if (Fl == FF && Gi == GG && d.P - 1 == LP && ++nl) k_inner<FF, GG, LP><<<gi, FF * GG / 4, 0, p->stream>>>(p->dslots, d);
+    if (Fl == FF && Gi == GG && d.P - 1 == LP && ++nl) k_inner<FF, GG, LP><<<gi, FF * GG / 4, 0, p->stream>>>(p->dslots, base, d);
         PG_INNER2(16, 8, 1) PG_INNER2(32, 4, 1) PG_INNER2(32, 8, 1) PG_INNER2(64, 2, 1) PG_INNER2(64, 8, 1)
         PG_INNER2(128, 2, 1) PG_INNER2(128, 4, 1)
         PG_INNER2(32, 4, 2) PG_INNER2(32, 8, 2) PG_INNER2(64, 2, 2) PG_INNER2(64, 8, 2)
 #undef PG_INNER2
     } else {
-        const dim3 gm(d.M / (d.F[1] * Gm), p->S);
-#define PG_MID2(FF, GG)                                                                      \
-    if (d.F[1] == FF && Gm == GG && ++nl) {                                                 \
-        if (part == 1) k_mid_fwd<FF, GG><<<gm, FF * GG / 4, 0, p->stream>>>(p->dslots, d);  \
-        else k_mid_inv<FF, GG><<<gm, FF * GG / 4, 0, p->stream>>>(p->dslots, d);            \
+        if (d.P != 3) return PG_EINVAL;
+        const dim3 gm(d.M / (d.F[1] * Gm), count);
+#define PG_MID2(FF, GG)                                                                            \
+    if (d.F[1] == FF && Gm == GG && ++nl) {                                                       \
+        if (part == 1) k_mid_fwd<FF, GG><<<gm, FF * GG / 4, 0, p->stream>>>(p->dslots, base, d);  \
+        else k_mid_inv<FF, GG><<<gm, FF * GG / 4, 0, p->stream>>>(p->dslots, base, d);            \
     }
         PG_MID2(32, 2) PG_MID2(32, 8) PG_MID2(64, 2) PG_MID2(64, 8)
 #undef PG_MID2
     }
+    if (part != 0 && part != parts - 1 && nl != 1) return PG_EINVAL;  // no kernel instance for this shape
     PG_CK(cudaGetLastError());
+    if (!p->capturing) g_launches++;
     return PG_OK;
 }
 
 static void pool_free(Pool* p) {
     if (!p) return;
-    if (p->graph) cudaGraphExecDestroy(p->graph);
+    for (auto& kv : p->graphs) cudaGraphExecDestroy(kv.second);
     for (int s = 0; s < p->S; ++s)
         if (p->slot_n[s]) put_weights(p->slot_n[s], p->M);
     cudaFree(p->digits);
@@ -458,22 +427,32 @@ static int pool_load(Pool* p, int s, const Limbs& x, uint64_t k, unsigned n, con
                           cudaMemcpyHostToDevice, p->stream));
     p->h_st[s] = st0;
     p->h_st[s].top = 0;
+    p->h_st[s].pend_lo = 0;
+    p->h_st[s].pend_hi = 0;
+    p->h_st[s].op = OP_PRODUCT;
+    p->h_st[s].partner = s;
     PG_CK(cudaMemcpyAsync(p->st + s, &p->h_st[s], sizeof(SlotState), cudaMemcpyHostToDevice, p->stream));
     PG_CK(cudaStreamSynchronize(p->stream));  // car is a host temporary
     return PG_OK;
 }
 
-// Canonical x of every slot (resolves pending carries on the device).
-static int pool_readback(Pool* p) {
+// Canonical digits of slots [base, base+count) into the pinned staging
+// buffers (resolves pending carries on the device; slot state unchanged).
+static int pool_readback(Pool* p, int base = 0, int count = -1) {
+    if (count < 0) count = p->S - base;
     const PlanDev& d = p->plan->dev;
     const int nruns = d.M / RUN;
-    const dim3 g((nruns + 127) / 128, p->S);
-    k_readback<<<g, 128, 0, p->stream>>>(p->dslots, d, p->rb_digits, p->rb_top);
+    const dim3 g((nruns + 127) / 128, count);
+    k_readback<<<g, 128, 0, p->stream>>>(p->dslots, base, d, p->rb_digits, p->rb_top);
     PG_CK(cudaGetLastError());
-    PG_CK(cudaMemcpyAsync(p->h_rb_digits, p->rb_digits, (size_t)p->S * d.M * sizeof(int), cudaMemcpyDeviceToHost,
+    g_launches++;
+    const size_t off = (size_t)base * d.M;
+    PG_CK(cudaMemcpyAsync(p->h_rb_digits + off, p->rb_digits + off, (size_t)count * d.M * sizeof(int),
+                          cudaMemcpyDeviceToHost, p->stream));
+    PG_CK(cudaMemcpyAsync(p->h_rb_top + base, p->rb_top + base, count * sizeof(long long), cudaMemcpyDeviceToHost,
                           p->stream));
-    PG_CK(cudaMemcpyAsync(p->h_rb_top, p->rb_top, p->S * sizeof(long long), cudaMemcpyDeviceToHost, p->stream));
-    PG_CK(cudaMemcpyAsync(p->h_st, p->st, p->S * sizeof(SlotState), cudaMemcpyDeviceToHost, p->stream));
+    PG_CK(cudaMemcpyAsync(p->h_st + base, p->st + base, count * sizeof(SlotState), cudaMemcpyDeviceToHost,
+                          p->stream));
     PG_CK(cudaStreamSynchronize(p->stream));
     return PG_OK;
 }
@@ -484,27 +463,37 @@ static Limbs slot_value(Pool* p, int s) {
     return from_mont(y, sl.k, sl.n);
 }
 
-// Run `steps` kernel-sequence steps on the pool stream (graph replay when possible).
-static int pool_run(Pool* p, long long steps, bool use_graph) {
-    const int GSTEPS = 50;
-    if (use_graph && steps >= GSTEPS && !p->graph) {
-        cudaGraph_t g;
-        PG_CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = PG_OK;
-        for (int i = 0; i < GSTEPS && rc == PG_OK; ++i) rc = enqueue_step(p);
-        cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
-        if (rc) return rc;
-        PG_CK(ce);
-        PG_CK(cudaGraphInstantiate(&p->graph, g, 0));
-        cudaGraphDestroy(g);
-        p->graph_steps = GSTEPS;
+// Run `steps` kernel-sequence steps on slots [base, base+count) (graph replay when possible).
+static int pool_run(Pool* p, long long steps, bool use_graph, int base = 0, int count = -1) {
+    if (count < 0) count = p->S;
+    const auto key = std::make_pair(base, count);
+    cudaGraphExec_t ge = nullptr;
+    if (use_graph && steps >= GSTEPS) {
+        auto it = p->graphs.find(key);
+        if (it != p->graphs.end()) {
+            ge = it->second;
+        } else {
+            cudaGraph_t g;
+            PG_CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+            int rc = PG_OK;
+            p->capturing = true;
+            for (int i = 0; i < GSTEPS && rc == PG_OK; ++i) rc = enqueue_step(p, base, count);
+            p->capturing = false;
+            cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
+            if (rc) return rc;
+            PG_CK(ce);
+            PG_CK(cudaGraphInstantiate(&ge, g, 0));
+            cudaGraphDestroy(g);
+            p->graphs[key] = ge;
+        }
     }
     while (steps > 0) {
-        if (use_graph && p->graph && steps >= p->graph_steps) {
-            PG_CK(cudaGraphLaunch(p->graph, p->stream));
-            steps -= p->graph_steps;
+        if (ge && steps >= GSTEPS) {
+            PG_CK(cudaGraphLaunch(ge, p->stream));
+            g_launches += (unsigned long long)GSTEPS * (p->plan->dev.P == 3 ? 5 : 3);
+            steps -= GSTEPS;
         } else {
-            int rc = enqueue_step(p);
+            int rc = enqueue_step(p, base, count);
             if (rc) return rc;
             steps -= 1;
         }
@@ -518,35 +507,71 @@ static double bits_to_double(unsigned long long b) {
     return d;
 }
 
-}  // namespace pg
-
-using namespace pg;
+// FP64 FMA throughput probe: 8 independent DFMA chains per thread.
+__global__ void k_dfma_peak(double* out, int iters, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = threadIdx.x * 1e-9 + i;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) x[i] = fma(x[i], a, b);
+    }
+    double s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += x[i];
+    if (s == 1234.5) out[0] = s;
+}
 
 // ---------------------------------------------------------------------------
 // single-candidate engine
+
+// Slots of a single-candidate engine's pool.  With the Gerbicz check on:
+//   X  the residue          D   product of block-end residues since X0
+//   Y  scratch: the previous D, then the verification value
+//   X0 last verified residue XB residue at the start of the current block
+enum { SX = 0, SD = 1, SY = 2, SX0 = 3, SXB = 4, NSLOTS_GZ = 5 };
+
+__global__ void k_copy_state(const Slot* __restrict__ slots, int src, int dst) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        SlotState s = *slots[src].st;
+        s.op = OP_PRODUCT;
+        s.partner = dst;
+        *slots[dst].st = s;
+    }
+}
+
+}  // namespace pg
 
 struct pg_engine {
     uint64_t k = 0;
     unsigned n = 0;
     unsigned flags = 0;
     int lg = 0;
-    Pool* pool = nullptr;
-    // rollback snapshot (device) of the slot
+    int nslots = 1;
+    pg::Pool* pool = nullptr;
+    // rollback snapshot (device) of one slot, taken per chunk
     int* snap_digits = nullptr;
     long long* snap_carries = nullptr;
-    SlotState* snap_st = nullptr;
+    pg::SlotState* snap_st = nullptr;
     double max_err = 0.0;
     uint64_t squarings = 0;
     uint32_t checks = 0, failures = 0, bumps = 0;
-    uint32_t gerbicz_block = 1000, gerbicz_every = 0;
+    // Gerbicz-Li check: D_t = X0 * D_{t-1}^(2^B) over blocks of B squarings
+    bool gz = false;
+    uint32_t B = 1000, V = 0;
+    bool armed = false;
+    uint64_t blocks = 0, in_block = 0;
+    uint32_t consecutive_fail = 0;
     bool loaded = false;
 };
 
+namespace pg {
+
 static int engine_alloc(pg_engine* e, int lg) {
     Pool* p = nullptr;
-    int rc = pool_create(lg, 1, &p);
+    int rc = pool_create(lg, e->nslots, &p);
     if (rc) return rc;
-    rc = pool_bind(p, 0, e->k, e->n);
+    for (int s = 0; s < e->nslots && !rc; ++s) rc = pool_bind(p, s, e->k, e->n);
     if (rc) {
         pool_free(p);
         return rc;
@@ -570,81 +595,104 @@ static int engine_alloc(pg_engine* e, int lg) {
     return PG_OK;
 }
 
-static int snapshot(pg_engine* e, bool restore) {
+static int slot_state(pg_engine* e, int s, SlotState* out) {
+    Pool* p = e->pool;
+    PG_CK(cudaMemcpyAsync(p->h_st + s, p->st + s, sizeof(SlotState), cudaMemcpyDeviceToHost, p->stream));
+    PG_CK(cudaStreamSynchronize(p->stream));
+    *out = p->h_st[s];
+    return PG_OK;
+}
+
+static int slot_write(pg_engine* e, int s, const SlotState& st) {
+    Pool* p = e->pool;
+    p->h_st[s] = st;
+    PG_CK(cudaMemcpyAsync(p->st + s, p->h_st + s, sizeof(SlotState), cudaMemcpyHostToDevice, p->stream));
+    PG_CK(cudaStreamSynchronize(p->stream));  // the pinned staging entry is reused
+    return PG_OK;
+}
+
+static int slot_copy(pg_engine* e, int src, int dst) {
+    if (src == dst) return PG_OK;
     Pool* p = e->pool;
     const size_t M = p->M, nruns = M / RUN;
-    const Slot& sl = p->hslots[0];
+    PG_CK(cudaMemcpyAsync(p->hslots[dst].digits, p->hslots[src].digits, M * sizeof(int), cudaMemcpyDeviceToDevice,
+                          p->stream));
+    PG_CK(cudaMemcpyAsync(p->hslots[dst].carries, p->hslots[src].carries, nruns * 2 * sizeof(long long),
+                          cudaMemcpyDeviceToDevice, p->stream));
+    k_copy_state<<<1, 32, 0, p->stream>>>(p->dslots, src, dst);
+    PG_CK(cudaGetLastError());
+    g_launches++;
+    return PG_OK;
+}
+
+static int slot_snapshot(pg_engine* e, int s, bool restore) {
+    Pool* p = e->pool;
+    const size_t M = p->M, nruns = M / RUN;
+    const Slot& sl = p->hslots[s];
+    const cudaMemcpyKind kind = cudaMemcpyDeviceToDevice;
     if (!restore) {
-        PG_CK(cudaMemcpyAsync(e->snap_digits, sl.digits, M * sizeof(int), cudaMemcpyDeviceToDevice, p->stream));
-        PG_CK(cudaMemcpyAsync(e->snap_carries, sl.carries, nruns * 2 * sizeof(long long), cudaMemcpyDeviceToDevice,
-                              p->stream));
-        PG_CK(cudaMemcpyAsync(e->snap_st, sl.st, sizeof(SlotState), cudaMemcpyDeviceToDevice, p->stream));
+        PG_CK(cudaMemcpyAsync(e->snap_digits, sl.digits, M * sizeof(int), kind, p->stream));
+        PG_CK(cudaMemcpyAsync(e->snap_carries, sl.carries, nruns * 2 * sizeof(long long), kind, p->stream));
+        PG_CK(cudaMemcpyAsync(e->snap_st, sl.st, sizeof(SlotState), kind, p->stream));
     } else {
-        PG_CK(cudaMemcpyAsync(sl.digits, e->snap_digits, M * sizeof(int), cudaMemcpyDeviceToDevice, p->stream));
-        PG_CK(cudaMemcpyAsync(sl.carries, e->snap_carries, nruns * 2 * sizeof(long long), cudaMemcpyDeviceToDevice,
-                              p->stream));
-        PG_CK(cudaMemcpyAsync(sl.st, e->snap_st, sizeof(SlotState), cudaMemcpyDeviceToDevice, p->stream));
+        PG_CK(cudaMemcpyAsync(sl.digits, e->snap_digits, M * sizeof(int), kind, p->stream));
+        PG_CK(cudaMemcpyAsync(sl.carries, e->snap_carries, nruns * 2 * sizeof(long long), kind, p->stream));
+        PG_CK(cudaMemcpyAsync(sl.st, e->snap_st, sizeof(SlotState), kind, p->stream));
     }
     return PG_OK;
 }
 
-static int read_state(pg_engine* e, SlotState* out) {
-    Pool* p = e->pool;
-    PG_CK(cudaMemcpyAsync(p->h_st, p->st, sizeof(SlotState), cudaMemcpyDeviceToHost, p->stream));
-    PG_CK(cudaStreamSynchronize(p->stream));
-    *out = p->h_st[0];
-    return PG_OK;
-}
-
-static int write_state(pg_engine* e, const SlotState& s) {
-    Pool* p = e->pool;
-    p->h_st[0] = s;
-    PG_CK(cudaMemcpyAsync(p->st, p->h_st, sizeof(SlotState), cudaMemcpyHostToDevice, p->stream));
-    return PG_OK;
-}
-
-// Move the current residue to a larger FFT length (after roundoff > 0.4).
+// Move every slot to the next FFT length (after roundoff > 0.4).
 static int engine_bump(pg_engine* e) {
     if (e->lg >= kMaxLg || (e->flags & PG_FLAG_NO_BUMP)) return PG_EROUNDOFF;
     if ((double)e->n / (double)(2u << e->lg) < kMinBitsPerDigit) return PG_EROUNDOFF;
     int rc = pool_readback(e->pool);
     if (rc) return rc;
-    const Limbs x = slot_value(e->pool, 0);
-    SlotState st = e->pool->h_st[0];
+    std::vector<Limbs> vals(e->nslots);
+    std::vector<SlotState> sts(e->nslots);
+    for (int s = 0; s < e->nslots; ++s) {
+        vals[s] = slot_value(e->pool, s);
+        sts[s] = e->pool->h_st[s];
+    }
     rc = engine_alloc(e, e->lg + 1);
     if (rc) return rc;
-    st.maxerr_bits = 0;
-    st.flags = 0;
-    rc = pool_load(e->pool, 0, x, e->k, e->n, st);
+    for (int s = 0; s < e->nslots && !rc; ++s) {
+        sts[s].maxerr_bits = 0;
+        sts[s].flags = 0;
+        rc = pool_load(e->pool, s, vals[s], e->k, e->n, sts[s]);
+    }
     if (rc) return rc;
     e->bumps++;
     return PG_OK;
 }
 
-// Advance `steps` schedule steps with roundoff monitoring, chunk-wise rollback and bumps.
-static int engine_advance(pg_engine* e, uint64_t steps) {
+// Square slot s `steps` times, chunk by chunk: each chunk is checked for
+// roundoff > 0.4 and digit overflow; a bad chunk is rolled back and redone at
+// the next FFT length.
+static int run_squarings(pg_engine* e, int s, uint64_t steps) {
     const uint64_t CHUNK = 2000;
     int guard = 0;
     while (steps > 0) {
         const uint64_t c = std::min<uint64_t>(steps, CHUNK);
         SlotState st;
-        int rc = read_state(e, &st);
+        int rc = slot_state(e, s, &st);
         if (rc) return rc;
-        rc = snapshot(e, false);
+        rc = slot_snapshot(e, s, false);
         if (rc) return rc;
         st.total = st.step + (long long)c;
         st.maxerr_bits = 0;
-        rc = write_state(e, st);
+        st.op = OP_PRODUCT;
+        st.partner = s;
+        rc = slot_write(e, s, st);
         if (rc) return rc;
-        rc = pool_run(e->pool, (long long)c, !(e->flags & PG_FLAG_NO_GRAPH));
+        rc = pool_run(e->pool, (long long)c, !(e->flags & PG_FLAG_NO_GRAPH), s, 1);
         if (rc) return rc;
         SlotState after;
-        rc = read_state(e, &after);
+        rc = slot_state(e, s, &after);
         if (rc) return rc;
         const double err = bits_to_double(after.maxerr_bits);
         if (err > 0.4 || after.flags != 0 || after.step != st.total) {
-            // roll back this chunk and retry at the next FFT length
-            rc = snapshot(e, true);
+            rc = slot_snapshot(e, s, true);
             if (rc) return rc;
             PG_CK(cudaStreamSynchronize(e->pool->stream));
             rc = engine_bump(e);
@@ -653,11 +701,191 @@ static int engine_advance(pg_engine* e, uint64_t steps) {
             continue;
         }
         e->max_err = std::max(e->max_err, err);
-        e->squarings += c;
         steps -= c;
     }
     return PG_OK;
 }
+
+// a <- a * b * 2^-n (Montgomery product); a and b are adjacent slots.
+// Returns PG_EROUNDOFF when the product's roundoff or digits went out of range.
+static int run_product(pg_engine* e, int a, int b) {
+    if (a - b != 1 && b - a != 1) return PG_EINVAL;
+    SlotState sa, sb;
+    int rc = slot_state(e, a, &sa);
+    if (!rc) rc = slot_state(e, b, &sb);
+    if (rc) return rc;
+    sa.total = sa.step + 1;
+    sa.op = OP_PRODUCT;
+    sa.partner = b;
+    sa.kexp = 0;
+    sa.maxerr_bits = 0;
+    sb.total = sb.step + 1;
+    sb.op = OP_FORWARD;
+    sb.partner = b;
+    rc = slot_write(e, a, sa);
+    if (!rc) rc = slot_write(e, b, sb);
+    if (!rc) rc = pool_run(e->pool, 1, false, std::min(a, b), 2);
+    if (rc) return rc;
+    SlotState ra, rb;
+    rc = slot_state(e, a, &ra);
+    if (!rc) rc = slot_state(e, b, &rb);
+    if (rc) return rc;
+    ra.partner = a;
+    rb.op = OP_PRODUCT;
+    rb.partner = b;
+    rc = slot_write(e, a, ra);
+    if (!rc) rc = slot_write(e, b, rb);
+    if (rc) return rc;
+    const double err = bits_to_double(ra.maxerr_bits);
+    if (err > 0.4 || ra.flags != 0 || rb.flags != 0) return PG_EROUNDOFF;
+    e->max_err = std::max(e->max_err, err);
+    return PG_OK;
+}
+
+static int slots_equal(pg_engine* e, int a, int b, bool* eq) {
+    int rc = pool_readback(e->pool, std::min(a, b), std::abs(a - b) + 1);
+    if (rc) return rc;
+    *eq = slot_value(e->pool, a) == slot_value(e->pool, b);
+    return PG_OK;
+}
+
+static int gz_arm(pg_engine* e, int from) {
+    int rc = PG_OK;
+    for (int dst : {SX0, SD, SXB})
+        if (!rc && dst != from) rc = slot_copy(e, from, dst);
+    e->blocks = 0;
+    e->armed = true;
+    return rc;
+}
+
+// Back to the last verified residue; returns the squarings to redo.
+static uint64_t gz_rollback(pg_engine* e, int* rc) {
+    const uint64_t redo = e->blocks * e->B + e->in_block;
+    *rc = slot_copy(e, SX0, SX);
+    if (!*rc) *rc = gz_arm(e, SX0);
+    e->in_block = 0;
+    e->failures++;
+    e->consecutive_fail++;
+    e->squarings -= std::min<uint64_t>(e->squarings, redo);
+    return redo;
+}
+
+// Verify the completed blocks: Y holds D_{t-1}; check X0 * Y^(2^B) == D.
+static int gz_verify_blocks(pg_engine* e, bool* ok) {
+    *ok = true;
+    if (e->blocks == 0) return PG_OK;
+    int rc = run_squarings(e, SY, e->B);
+    if (rc) return rc;
+    rc = run_product(e, SY, SX0);
+    if (rc == PG_EROUNDOFF) {
+        *ok = false;
+        return PG_OK;
+    }
+    if (rc) return rc;
+    rc = slots_equal(e, SY, SD, ok);
+    if (rc) return rc;
+    if (*ok) {
+        e->checks++;
+        e->consecutive_fail = 0;
+        rc = gz_arm(e, SXB);  // the end of the last full block is now verified
+    }
+    return rc;
+}
+
+static int gz_square(pg_engine* e, uint64_t iters) {
+    if (!e->armed) {
+        int rc = gz_arm(e, SX);
+        if (rc) return rc;
+        e->in_block = 0;
+    }
+    uint64_t owed = iters;
+    while (owed > 0) {
+        if (e->consecutive_fail > 4) return PG_EGERBICZ;
+        const uint64_t c = std::min<uint64_t>(owed, e->B - e->in_block);
+        int rc = run_squarings(e, SX, c);
+        if (rc) return rc;
+        e->in_block += c;
+        e->squarings += c;
+        owed -= c;
+        if (e->in_block == e->B) {
+            // block end: Y = D_{t-1}, D = D * X, XB = X
+            rc = slot_copy(e, SD, SY);
+            if (!rc) rc = run_product(e, SD, SX);
+            if (rc == PG_EROUNDOFF) {
+                owed += gz_rollback(e, &rc);
+                if (rc) return rc;
+                continue;
+            }
+            if (rc) return rc;
+            rc = slot_copy(e, SX, SXB);
+            if (rc) return rc;
+            e->blocks++;
+            e->in_block = 0;
+            if (e->V && e->blocks >= e->V) {
+                bool ok = true;
+                rc = gz_verify_blocks(e, &ok);
+                if (rc) return rc;
+                if (!ok) {
+                    owed += gz_rollback(e, &rc);
+                    if (rc) return rc;
+                }
+            }
+        }
+    }
+    return PG_OK;
+}
+
+// Verify everything since the last verified residue, including a partial
+// block (recomputed from XB); on a mismatch, roll back and redo.
+static int gz_flush(pg_engine* e) {
+    if (!e->gz || !e->armed) return PG_OK;
+    for (int guard = 0; guard < 16; ++guard) {
+        int rc = PG_OK;
+        if (e->blocks > 0) {
+            bool ok = true;
+            rc = gz_verify_blocks(e, &ok);
+            if (rc) return rc;
+            if (!ok) {
+                const uint64_t redo = gz_rollback(e, &rc);
+                if (!rc) rc = gz_square(e, redo);
+                if (rc) return rc;
+                continue;
+            }
+        }
+        if (e->in_block > 0) {
+            rc = slot_copy(e, SXB, SY);
+            if (!rc) rc = run_squarings(e, SY, e->in_block);
+            bool ok = false;
+            if (!rc) rc = slots_equal(e, SY, SX, &ok);
+            if (rc) return rc;
+            if (ok) {
+                e->checks++;
+                e->consecutive_fail = 0;
+                e->in_block = 0;
+                rc = gz_arm(e, SX);
+                if (rc) return rc;
+            } else {
+                const uint64_t redo = e->in_block;
+                rc = slot_copy(e, SXB, SX);
+                if (rc) return rc;
+                e->in_block = 0;
+                e->failures++;
+                e->consecutive_fail++;
+                e->squarings -= std::min<uint64_t>(e->squarings, redo);
+                if (e->consecutive_fail > 4) return PG_EGERBICZ;
+                rc = gz_square(e, redo);
+                if (rc) return rc;
+                continue;
+            }
+        }
+        if (e->blocks == 0 && e->in_block == 0) return PG_OK;
+    }
+    return PG_EGERBICZ;
+}
+
+}  // namespace pg
+
+using namespace pg;
 
 extern "C" {
 
@@ -723,15 +951,18 @@ int pg_create(uint64_t k, uint32_t n, uint32_t fft_len_hint, uint32_t flags, pg_
         while ((1u << h) < fft_len_hint) ++h;
         lg = (flags & PG_FLAG_FORCE_LEN) ? h : std::max(lg, h);
     }
-    if (lg >= kMinLg && (double)n / (double)(1 << lg) < kMinBitsPerDigit) return PG_EINVAL;
     if (lg < 0 || lg > kMaxLg) return PG_EINVAL;
     lg = std::max(lg, kMinLg);
+    if ((double)n / (double)(1 << lg) < kMinBitsPerDigit) return PG_EINVAL;
+    if ((double)n / (double)(1 << lg) > kMaxBitsPerDigit) return PG_EINVAL;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PG_ENODEV;
     pg_engine* e = new pg_engine();
     e->k = k;
     e->n = n;
     e->flags = flags;
+    e->gz = !(flags & PG_FLAG_NO_GERBICZ);
+    e->nslots = e->gz ? NSLOTS_GZ : 1;
     int rc = engine_alloc(e, lg);
     if (rc) {
         delete e;
@@ -758,18 +989,23 @@ int pg_set_residue(pg_engine* e, const uint64_t* limbs, size_t n_limbs) {
     SlotState st;
     memset(&st, 0, sizeof(st));
     st.mul = 1;
-    int rc = pool_load(e->pool, 0, x, e->k, e->n, st);
+    int rc = pool_load(e->pool, SX, x, e->k, e->n, st);
     if (rc) return rc;
     e->loaded = true;
+    e->armed = false;  // the Gerbicz check restarts from this residue
+    e->in_block = 0;
+    e->blocks = 0;
     return PG_OK;
 }
 
 int pg_get_residue(pg_engine* e, uint64_t* limbs, size_t n_limbs) {
     if (!e || !limbs) return PG_EINVAL;
     if (!e->loaded) return PG_ESTATE;
-    int rc = pool_readback(e->pool);
+    int rc = gz_flush(e);  // a returned residue is always a verified one
     if (rc) return rc;
-    const Limbs x = slot_value(e->pool, 0);
+    rc = pool_readback(e->pool, SX, 1);
+    if (rc) return rc;
+    const Limbs x = slot_value(e->pool, SX);
     if (x.size() > n_limbs) return PG_EINVAL;
     memset(limbs, 0, n_limbs * sizeof(uint64_t));
     std::copy(x.begin(), x.end(), limbs);
@@ -779,7 +1015,14 @@ int pg_get_residue(pg_engine* e, uint64_t* limbs, size_t n_limbs) {
 int pg_square(pg_engine* e, uint64_t iters) {
     if (!e) return PG_EINVAL;
     if (!e->loaded) return PG_ESTATE;
-    return engine_advance(e, iters);
+    if (!e->gz) {
+        const int rc = run_squarings(e, SX, iters);
+        if (!rc) e->squarings += iters;
+        return rc;
+    }
+    int rc = gz_square(e, iters);
+    if (!rc && e->V == 0) rc = gz_flush(e);
+    return rc;
 }
 
 int pg_pow_small(pg_engine* e, uint64_t base_a, uint64_t exponent) {
@@ -792,17 +1035,35 @@ int pg_pow_small(pg_engine* e, uint64_t base_a, uint64_t exponent) {
     int rc = pg_set_residue(e, &a, 1);
     if (rc) return rc;
     SlotState st;
-    rc = read_state(e, &st);
+    rc = slot_state(e, SX, &st);
     if (rc) return rc;
     st.kexp = exponent;
     st.kbits = (int)bitlen(exponent);
     st.mul = (int)base_a;
-    rc = write_state(e, st);
+    rc = slot_write(e, SX, st);
     if (rc) return rc;
-    const uint64_t before = e->squarings;
-    rc = engine_advance(e, (uint64_t)st.kbits - 1);
-    e->squarings = before;  // the powering steps are not squarings of the test loop
-    return rc;
+    // the powering chain is short (bitlen(exponent) - 1 steps); it is checked
+    // for roundoff like any chunk, and verified by recomputation below
+    rc = run_squarings(e, SX, (uint64_t)st.kbits - 1);
+    if (rc || !e->gz) return rc;
+    // independent recomputation in slot Y, compared with X
+    const uint64_t a2 = base_a;
+    SlotState sy;
+    memset(&sy, 0, sizeof(sy));
+    sy.kexp = exponent;
+    sy.kbits = (int)bitlen(exponent);
+    sy.mul = (int)base_a;
+    rc = pool_load(e->pool, SY, Limbs(1, a2), e->k, e->n, sy);
+    if (!rc) rc = run_squarings(e, SY, (uint64_t)st.kbits - 1);
+    bool ok = false;
+    if (!rc) rc = slots_equal(e, SX, SY, &ok);
+    if (rc) return rc;
+    if (!ok) {
+        e->failures++;
+        return PG_EGERBICZ;
+    }
+    e->checks++;
+    return PG_OK;
 }
 
 int pg_max_err(pg_engine* e, double* out, int reset) {
@@ -820,8 +1081,12 @@ int pg_fft_len(const pg_engine* e, uint32_t* out) {
 
 int pg_set_gerbicz(pg_engine* e, uint32_t block, uint32_t verify_every_blocks) {
     if (!e || block == 0) return PG_EINVAL;
-    e->gerbicz_block = block;
-    e->gerbicz_every = verify_every_blocks;
+    if (!e->gz) return PG_ESTATE;
+    int rc = gz_flush(e);
+    if (rc) return rc;
+    e->B = block;
+    e->V = verify_every_blocks;
+    e->armed = false;
     return PG_OK;
 }
 
@@ -838,16 +1103,18 @@ int pg_time_squarings(pg_engine* e, uint64_t iters, double* ms, uint32_t* kernel
     if (!e || !ms) return PG_EINVAL;
     if (!e->loaded) return PG_ESTATE;
     SlotState st;
-    int rc = read_state(e, &st);
+    int rc = slot_state(e, SX, &st);
     if (rc) return rc;
     st.total = st.step + (long long)iters;
-    rc = write_state(e, st);
+    st.op = OP_PRODUCT;
+    st.partner = SX;
+    rc = slot_write(e, SX, st);
     if (rc) return rc;
     cudaEvent_t a, b;
     PG_CK(cudaEventCreate(&a));
     PG_CK(cudaEventCreate(&b));
     PG_CK(cudaEventRecord(a, e->pool->stream));
-    rc = pool_run(e->pool, (long long)iters, !(e->flags & PG_FLAG_NO_GRAPH));
+    rc = pool_run(e->pool, (long long)iters, !(e->flags & PG_FLAG_NO_GRAPH), SX, 1);
     PG_CK(cudaEventRecord(b, e->pool->stream));
     PG_CK(cudaEventSynchronize(b));
     float f = 0.f;
@@ -856,6 +1123,7 @@ int pg_time_squarings(pg_engine* e, uint64_t iters, double* ms, uint32_t* kernel
     cudaEventDestroy(b);
     *ms = f;
     if (kernels_per_step) *kernels_per_step = e->pool->plan->dev.P == 3 ? 5 : 3;
+    e->armed = false;  // squarings outside the Gerbicz bookkeeping
     if (!rc) e->squarings += iters;
     return rc;
 }
@@ -864,17 +1132,19 @@ int pg_profile_step(pg_engine* e, double* times, uint32_t cap, uint32_t* count) 
     if (!e || !times || !count) return PG_EINVAL;
     if (!e->loaded) return PG_ESTATE;
     SlotState st;
-    int rc = read_state(e, &st);
+    int rc = slot_state(e, SX, &st);
     if (rc) return rc;
     st.total = st.step + 1;
-    rc = write_state(e, st);
+    st.op = OP_PRODUCT;
+    st.partner = SX;
+    rc = slot_write(e, SX, st);
     if (rc) return rc;
     const int parts = e->pool->plan->dev.P == 3 ? 5 : 3;
     std::vector<cudaEvent_t> ev(parts + 1);
     for (auto& x : ev) PG_CK(cudaEventCreate(&x));
     PG_CK(cudaEventRecord(ev[0], e->pool->stream));
     for (int i = 0; i < parts && rc == PG_OK; ++i) {
-        rc = enqueue_step_part(e->pool, i);
+        rc = enqueue_step_part(e->pool, i, SX, 1);
         cudaEventRecord(ev[i + 1], e->pool->stream);
     }
     PG_CK(cudaEventSynchronize(ev[parts]));
@@ -886,13 +1156,79 @@ int pg_profile_step(pg_engine* e, double* times, uint32_t cap, uint32_t* count) 
         *count = i + 1;
     }
     for (auto& x : ev) cudaEventDestroy(x);
+    e->armed = false;
     if (!rc) e->squarings += 1;
     return rc;
 }
 
+int pg_square_timed(pg_engine* e, uint64_t iters, double* ms) {
+    if (!e || !ms) return PG_EINVAL;
+    cudaEvent_t a, b;
+    PG_CK(cudaEventCreate(&a));
+    PG_CK(cudaEventCreate(&b));
+    PG_CK(cudaEventRecord(a, e->pool->stream));
+    const int rc = pg_square(e, iters);
+    // pg_square may have replaced the pool (FFT-length bump): record on the current stream
+    PG_CK(cudaEventRecord(b, e->pool->stream));
+    PG_CK(cudaEventSynchronize(b));
+    float f = 0.f;
+    cudaEventElapsedTime(&f, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = f;
+    return rc;
+}
+
+static void* g_flush_buf = nullptr;
+static const size_t kFlushBytes = 512ull << 20;  // 4x the 129 MB L2
+
+int pg_flush_l2(void) {
+    if (!g_flush_buf) PG_CK(cudaMalloc(&g_flush_buf, kFlushBytes));
+    PG_CK(cudaMemset(g_flush_buf, 0x5a, kFlushBytes));
+    PG_CK(cudaDeviceSynchronize());
+    return PG_OK;
+}
+
+uint64_t pg_launch_count(void) { return g_launches.load(); }
+
+int pg_set_device(int device) {
+    PG_CK(cudaSetDevice(device));
+    return PG_OK;
+}
+
+int pg_measure_fp64_peak(double* tflops) {
+    if (!tflops) return PG_EINVAL;
+    int dev = 0, sms = 0;
+    PG_CK(cudaGetDevice(&dev));
+    PG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    double* d = nullptr;
+    PG_CK(cudaMalloc(&d, 64));
+    cudaEvent_t a, b;
+    PG_CK(cudaEventCreate(&a));
+    PG_CK(cudaEventCreate(&b));
+    const int blocks = 4 * sms, threads = 256, iters = 4000;
+    k_dfma_peak<<<blocks, threads>>>(d, 100, 1.0000001, 1e-9);
+    g_launches += 4;
+    float best = 1e30f;
+    for (int r = 0; r < 3; ++r) {
+        cudaEventRecord(a);
+        k_dfma_peak<<<blocks, threads>>>(d, iters, 1.0000001, 1e-9);
+        cudaEventRecord(b);
+        PG_CK(cudaEventSynchronize(b));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        best = std::min(best, ms);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(d);
+    *tflops = 2.0 * 8.0 * (double)blocks * threads * iters / (best * 1e-3) / 1e12;
+    return PG_OK;
+}
+
 int pg_debug_corrupt(pg_engine* e, uint32_t index, int32_t delta) {
     if (!e || index >= e->pool->M) return PG_EINVAL;
-    k_corrupt<<<1, 32, 0, e->pool->stream>>>(e->pool->dslots, 0, index, delta);
+    k_corrupt<<<1, 32, 0, e->pool->stream>>>(e->pool->dslots, SX, index, delta);
     PG_CK(cudaGetLastError());
     PG_CK(cudaStreamSynchronize(e->pool->stream));
     return PG_OK;

@@ -25,8 +25,8 @@ constexpr int MAX_PASSES = 3;
 
 // Per-slot mutable state (device memory).
 struct SlotState {
-    long long step;                  // squarings completed
-    long long total;                 // squarings to reach; the slot idles at step == total
+    long long step;                  // operations completed
+    long long total;                 // operations to reach; the slot idles at step == total
     unsigned long long kexp;         // exponent driving the small-multiplier schedule (0 = none)
     int kbits;                       // bit length of kexp
     int mul;                         // small multiplier (the base a)
@@ -34,7 +34,15 @@ struct SlotState {
     int flags;                       // error bits (overflow, bad rounding range)
     unsigned long long maxerr_bits;  // max roundoff error, as the bits of a non-negative double
     long long top;                   // top digit of the current input (weight 2^n)
-    long long pad_;
+    long long pend_lo;               // pending contribution at weight 2^n (int128, lo/hi):
+    long long pend_hi;               //   s*top_a*top_b of the last product, or the re-armed top
+    int op;                          // OP_PRODUCT or OP_FORWARD
+    int partner;                     // slot whose digits/spectrum multiply this one (self: square)
+};
+
+enum SlotOp : int {
+    OP_PRODUCT = 0,  // y <- s * y * partner * 2^-n  (partner == self: square)
+    OP_FORWARD = 1   // operand of another slot's product: fix up + forward passes only
 };
 
 enum SlotFlags : int { SF_DIGIT_OVERFLOW = 1, SF_ROUND_RANGE = 2 };

@@ -202,17 +202,24 @@ __device__ __forceinline__ i128 floor_div(i128 a, i128 b) {  // b > 0
     return q;
 }
 
+__device__ __forceinline__ i128 load_pend(const SlotState* st) {
+    return (i128)(((unsigned __int128)(unsigned long long)st->pend_hi << 64) | (unsigned long long)st->pend_lo);
+}
+__device__ __forceinline__ void store_pend(SlotState* st, i128 v) {
+    st->pend_lo = (long long)(unsigned long long)v;
+    st->pend_hi = (long long)(v >> 64);
+}
+
 // Carry entering run `run` of a slot.  For run 0 it is minus the quotient of
-// the top-digit reduction: top' = s_prev top^2 + (carry out of the last run)
-// is split as q k + t with |t| <= k/2, and q k 2^n = -q (mod N).
+// the top-digit reduction: top' = pend + (carry out of the last run), where
+// pend = s top_a top_b of the last product, is split as q k + t with
+// |t| <= k/2, and q k 2^n = -q (mod N).
 __device__ __forceinline__ i128 run_carry_in(const Slot& sl, long long run, long long nruns,
-                                             long long step, long long* new_top) {
+                                             long long* new_top) {
     if (run > 0) return load_carry(sl.carries, run - 1);
     const SlotState* st = sl.st;
     const i128 clast = load_carry(sl.carries, nruns - 1);
-    const long long top = st->top;
-    const int sp = (step > 0) ? sched_mul(st, step - 1) : 1;
-    const i128 tp = (i128)sp * (i128)top * (i128)top + clast;
+    const i128 tp = load_pend(st) + clast;
     const i128 kk = (i128)sl.k;
     const i128 q = floor_div(2 * tp + kk, 2 * kk);
     *new_top = (long long)(tp - q * kk);
@@ -268,11 +275,11 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 // k_first: pass 0 forward.  CTA = RUN consecutive columns r (so each row of
 // the tile is one carry run) x F0 rows q; grid (S0 / RUN, slots).
 template <int F0>
-__global__ void __launch_bounds__(2 * F0) k_first(const Slot* __restrict__ slots, const PlanDev pl) {
+__global__ void __launch_bounds__(2 * F0) k_first(const Slot* __restrict__ slots, int base, const PlanDev pl) {
     constexpr int G = RUN, NT = 2 * F0;
     __shared__ double2 tile[F0 * G];
     __shared__ int dsm[F0 * G];
-    const Slot sl = slots[blockIdx.y];
+    const Slot sl = slots[base + blockIdx.y];
     SlotState* st = sl.st;
     const long long step = st->step;
     const bool act = step < st->total;
@@ -289,8 +296,16 @@ __global__ void __launch_bounds__(2 * F0) k_first(const Slot* __restrict__ slots
         const int4 v0 = dp[0], v1 = dp[1];
         int dv[RUN] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
         long long new_top = 0;
-        const i128 cin = run_carry_in(sl, run, nruns, step, &new_top);
-        if (run == 0) st->top = new_top;
+        const i128 cin = run_carry_in(sl, run, nruns, &new_top);
+        // each pending carry is consumed by exactly one run: zero it, and re-arm
+        // the top as pending, so a slot that only feeds another product stays exact
+        if (run == 0) {
+            st->top = new_top;
+            store_pend(st, (i128)new_top);
+            store_carry(sl.carries, nruns - 1, 0);
+        } else {
+            store_carry(sl.carries, run - 1, 0);
+        }
         int bad = 0;
         fixup_run(dv, cin, j0, sl.n, pl.lgM, bad);
         if (bad) atomicOr(&st->flags, SF_DIGIT_OVERFLOW);
@@ -319,19 +334,19 @@ __global__ void __launch_bounds__(2 * F0) k_first(const Slot* __restrict__ slots
 // k_mid_fwd / k_mid_inv: pass 1 of a three-pass plan.  CTA = G consecutive
 // columns of one block of length Mi[1]; grid (M / (F G), slots).
 template <int F, int G>
-__global__ void __launch_bounds__(F * G / 4) k_mid_fwd(const Slot* __restrict__ slots, const PlanDev pl) {
+__global__ void __launch_bounds__(F * G / 4) k_mid_fwd(const Slot* __restrict__ slots, int base, const PlanDev pl) {
     constexpr int NT = F * G / 4;
     __shared__ double2 tile[F * G];
-    const Slot sl = slots[blockIdx.y];
+    const Slot sl = slots[base + blockIdx.y];
     if (!sl.st->active) return;
     const int S = pl.S[1], Mi = pl.Mi[1];
     const int cpb = S / G;
     const int blk = blockIdx.x / cpb, r0 = (blockIdx.x % cpb) * G;
-    double2* base = sl.spec + (size_t)blk * Mi;
+    double2* bp = sl.spec + (size_t)blk * Mi;
     const int tid = threadIdx.x;
     for (int e = tid; e < F * G; e += NT) {
         const int q = e / G, t = e % G;
-        tile[e] = base[r0 + t + q * S];
+        tile[e] = bp[r0 + t + q * S];
     }
     __syncthreads();
     smem_fft_fwd<F, G, NT, false>(tile, pl.wF[1]);
@@ -339,69 +354,82 @@ __global__ void __launch_bounds__(F * G / 4) k_mid_fwd(const Slot* __restrict__ 
     for (int e = tid; e < F * G; e += NT) {
         const int p = e / G, t = e % G;
         const int r = r0 + t;
-        base[r + p * S] = cmul(tile[e], tw[p * S + r]);
+        bp[r + p * S] = cmul(tile[e], tw[p * S + r]);
     }
 }
 
 template <int F, int G>
-__global__ void __launch_bounds__(F * G / 4) k_mid_inv(const Slot* __restrict__ slots, const PlanDev pl) {
+__global__ void __launch_bounds__(F * G / 4) k_mid_inv(const Slot* __restrict__ slots, int base, const PlanDev pl) {
     constexpr int NT = F * G / 4;
     __shared__ double2 tile[F * G];
-    const Slot sl = slots[blockIdx.y];
-    if (!sl.st->active) return;
+    const Slot sl = slots[base + blockIdx.y];
+    if (!sl.st->active || sl.st->op == OP_FORWARD) return;
     const int S = pl.S[1], Mi = pl.Mi[1];
     const int cpb = S / G;
     const int blk = blockIdx.x / cpb, r0 = (blockIdx.x % cpb) * G;
-    double2* base = sl.spec + (size_t)blk * Mi;
+    double2* bp = sl.spec + (size_t)blk * Mi;
     const double2* __restrict__ tw = pl.tw[1];
     const int tid = threadIdx.x;
     for (int e = tid; e < F * G; e += NT) {
         const int p = e / G, t = e % G;
         const int r = r0 + t;
-        tile[e] = cmulc(base[r + p * S], tw[p * S + r]);
+        tile[e] = cmulc(bp[r + p * S], tw[p * S + r]);
     }
     __syncthreads();
     smem_fft_inv<F, G, NT, false>(tile, pl.wF[1]);
     for (int e = tid; e < F * G; e += NT) {
         const int q = e / G, t = e % G;
-        base[r0 + t + q * S] = tile[e];
+        bp[r0 + t + q * S] = tile[e];
     }
 }
 
-// k_inner: last pass.  CTA = G contiguous groups of F; forward, square, inverse.
+// k_inner: last pass.  CTA = G contiguous groups of F: forward, pointwise
+// product with the partner slot's spectrum (itself for a square), inverse.
 template <int F, int G, int LASTP>
-__global__ void __launch_bounds__(F * G / 4) k_inner(const Slot* __restrict__ slots, const PlanDev pl) {
+__global__ void __launch_bounds__(F * G / 4) k_inner(const Slot* __restrict__ slots, int base, const PlanDev pl) {
     constexpr int NT = F * G / 4;
     __shared__ double2 tile[F * G];
-    const Slot sl = slots[blockIdx.y];
+    __shared__ double2 tile2[F * G];
+    const Slot sl = slots[base + blockIdx.y];
     SlotState* st = sl.st;
     if (!st->active) return;
     const int tid = threadIdx.x;
     if (blockIdx.x == 0 && tid == 0) st->step += 1;  // nobody reads step until k_last
-    double2* base = sl.spec + (size_t)blockIdx.x * (F * G);
-    for (int e = tid; e < F * G; e += NT) tile[e] = base[e];
+    if (st->op == OP_FORWARD) return;                // the partner's k_inner transforms this slot
+    const int partner = st->partner;
+    const bool square = partner == base + (int)blockIdx.y;
+    double2* bp = sl.spec + (size_t)blockIdx.x * (F * G);
+    const double2* qp = slots[partner].spec + (size_t)blockIdx.x * (F * G);
+    for (int e = tid; e < F * G; e += NT) tile[e] = bp[e];
+    if (!square)
+        for (int e = tid; e < F * G; e += NT) tile2[e] = qp[e];
     __syncthreads();
     smem_fft_fwd<F, G, NT, true>(tile, pl.wF[LASTP]);
-    for (int e = tid; e < F * G; e += NT) {
-        const double2 z = tile[e];
-        tile[e] = make_double2(fma(z.x, z.x, -(z.y * z.y)), (z.x + z.x) * z.y);
+    if (square) {
+        for (int e = tid; e < F * G; e += NT) {
+            const double2 z = tile[e];
+            tile[e] = make_double2(fma(z.x, z.x, -(z.y * z.y)), (z.x + z.x) * z.y);
+        }
+    } else {
+        smem_fft_fwd<F, G, NT, true>(tile2, pl.wF[LASTP]);
+        for (int e = tid; e < F * G; e += NT) tile[e] = cmul(tile[e], tile2[e]);
     }
     __syncthreads();
     smem_fft_inv<F, G, NT, true>(tile, pl.wF[LASTP]);
-    for (int e = tid; e < F * G; e += NT) base[e] = tile[e];
+    for (int e = tid; e < F * G; e += NT) bp[e] = tile[e];
 }
 
 // k_last: pass 0 inverse + unweight + round + fold + carry within each run.
 template <int F0>
-__global__ void __launch_bounds__(2 * F0) k_last(const Slot* __restrict__ slots, const PlanDev pl) {
+__global__ void __launch_bounds__(2 * F0) k_last(const Slot* __restrict__ slots, int base, const PlanDev pl) {
     constexpr int G = RUN, NT = 2 * F0;
     __shared__ double2 tile[F0 * G];
     __shared__ long long cl[F0 * G];
     __shared__ long long ch[F0 * G];
     __shared__ unsigned long long wmax[NT / 32];
-    const Slot sl = slots[blockIdx.y];
+    const Slot sl = slots[base + blockIdx.y];
     SlotState* st = sl.st;
-    if (!st->active) return;
+    if (!st->active || st->op == OP_FORWARD) return;
     const int S0 = pl.S[0];
     const int r0 = blockIdx.x * G;
     const int tid = threadIdx.x;
@@ -436,18 +464,23 @@ __global__ void __launch_bounds__(2 * F0) k_last(const Slot* __restrict__ slots,
     if (tid < F0) {
         const unsigned long long j0 = (unsigned long long)r0 + (unsigned long long)tid * S0;
         const long long run = (long long)(j0 / RUN);
+        const Slot& pb = slots[st->partner];
         int4* dp = reinterpret_cast<int4*>(sl.digits + j0);
-        const int4 v0 = dp[0], v1 = dp[1];
+        const int4* qp = reinterpret_cast<const int4*>(pb.digits + j0);
+        const int4 v0 = dp[0], v1 = dp[1], w0 = qp[0], w1 = qp[1];
         const int dv[RUN] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
-        const i128 top2 = 2 * (i128)st->top;
+        const int dw[RUN] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+        const i128 ta = (i128)st->top, tb = (i128)pb.st->top;
         const i128 s = (i128)sched_mul(st, st->step - 1);
         const i128 kk = (i128)sl.k;
+        if (run == 0) store_pend(st, s * ta * tb);
         i128 carry = 0;
         int nd[RUN];
 #pragma unroll
         for (int t = 0; t < RUN; ++t) {
             const int e = tid * G + t;
-            const i128 u = s * ((i128)ch[e] + top2 * (i128)dv[t] - kk * (i128)cl[e]);
+            // X_a X_b 2^-n = H - k Lo; cross terms top_a X_b + top_b X_a sit at weight 2^n
+            const i128 u = s * ((i128)ch[e] + ta * (i128)dw[t] + tb * (i128)dv[t] - kk * (i128)cl[e]);
             carry += u;
             nd[t] = (int)take_digit(carry, digit_width(j0 + t, sl.n, pl.lgM));
         }
@@ -459,9 +492,9 @@ __global__ void __launch_bounds__(2 * F0) k_last(const Slot* __restrict__ slots,
 
 // k_readback: resolve the pending carries of each slot into out_digits /
 // out_top without changing the slot state.  One thread per run.
-__global__ void k_readback(const Slot* __restrict__ slots, const PlanDev pl, int* __restrict__ out_digits,
+__global__ void k_readback(const Slot* __restrict__ slots, int base, const PlanDev pl, int* __restrict__ out_digits,
                            long long* __restrict__ out_top) {
-    const Slot sl = slots[blockIdx.y];
+    const Slot sl = slots[base + blockIdx.y];
     const long long nruns = pl.M / RUN;
     const long long run = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (run >= nruns) return;
@@ -471,13 +504,13 @@ __global__ void k_readback(const Slot* __restrict__ slots, const PlanDev pl, int
 #pragma unroll
     for (int t = 0; t < RUN; ++t) dv[t] = dp[t];
     long long new_top = 0;
-    const i128 cin = run_carry_in(sl, run, nruns, sl.st->step, &new_top);
+    const i128 cin = run_carry_in(sl, run, nruns, &new_top);
     int bad = 0;
     fixup_run(dv, cin, j0, sl.n, pl.lgM, bad);
-    int* op = out_digits + (size_t)blockIdx.y * pl.M + j0;
+    int* op = out_digits + (size_t)(base + blockIdx.y) * pl.M + j0;
 #pragma unroll
     for (int t = 0; t < RUN; ++t) op[t] = dv[t];
-    if (run == 0) out_top[blockIdx.y] = new_top;
+    if (run == 0) out_top[base + blockIdx.y] = new_top;
     if (bad) atomicOr(&sl.st->flags, SF_DIGIT_OVERFLOW);
 }
 

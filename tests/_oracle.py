@@ -52,17 +52,11 @@ def lib():
 
 
 def to_limbs(x, nl):
-    a = (u64 * nl)()
-    for i in range(nl):
-        a[i] = (x >> (64 * i)) & 0xFFFFFFFFFFFFFFFF
-    return a
+    return (u64 * nl).from_buffer_copy(int(x).to_bytes(8 * nl, "little"))
 
 
 def from_limbs(a):
-    v = 0
-    for i in reversed(range(len(a))):
-        v = (v << 64) | int(a[i])
-    return v
+    return int.from_bytes(bytes(a), "little")
 
 
 class Ctx:

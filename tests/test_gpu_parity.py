@@ -163,20 +163,97 @@ def test_checkpoint_roundtrip(pg, tmp_path):
 def test_roundoff_bump_recovers(pg):
     """A forced, far too small FFT length overflows the rounding range; the
     engine rolls back, grows the length and still returns the exact residue."""
-    k, n = 999999, 65536
+    k, n = 999999, 45000  # 22 bits per digit at length 2048: products overflow FP64 rounding
     N = _N(k, n)
-    with pg.Engine(k, n, fft_len_hint=1024, flags=pg.FLAG_FORCE_LEN) as e:
-        assert e.fft_len == 1024
+    with pg.Engine(k, n, fft_len_hint=2048, flags=pg.FLAG_FORCE_LEN) as e:
+        assert e.fft_len == 2048
         e.set_residue(5)
         e.square(50)
         assert e.get_residue() == pow(5, 1 << 50, N)
         assert e.stats()["fft_bumps"] >= 1
-        assert e.fft_len > 1024
+        assert e.fft_len > 2048
+
+
+def test_digit_width_limits(pg):
+    with pytest.raises(pg.ProthGpuError):
+        pg.Engine(3, 65536, fft_len_hint=1024, flags=pg.FLAG_FORCE_LEN)  # 64-bit digits
+    with pytest.raises(pg.ProthGpuError):
+        pg.Engine(3, 1000)  # below 6 bits per digit at the smallest length
 
 
 def test_roundoff_without_bump_reports(pg):
-    with pg.Engine(999999, 65536, fft_len_hint=1024, flags=pg.FLAG_FORCE_LEN | pg.FLAG_NO_BUMP) as e:
+    with pg.Engine(999999, 45000, fft_len_hint=2048, flags=pg.FLAG_FORCE_LEN | pg.FLAG_NO_BUMP) as e:
         e.set_residue(5)
         with pytest.raises(pg.ProthGpuError) as ei:
             e.square(20)
         assert ei.value.status == pg.PG_EROUNDOFF
+
+
+def test_gerbicz_clean_run(pg):
+    k, n = 12345, 65536
+    N = _N(k, n)
+    with pg.Engine(k, n) as e:
+        e.set_gerbicz(100, 4)
+        e.set_residue(11)
+        e.square(1000)
+        st = e.stats()
+        assert st["gerbicz_checks"] >= 2 and st["gerbicz_failures"] == 0
+        assert e.get_residue() == pow(11, 1 << 1000, N)
+
+
+@pytest.mark.parametrize("when", [30, 250, 399])
+def test_gerbicz_detects_and_recovers_corruption(pg, when):
+    """A silent error in a residue digit (injected on the device, nothing
+    faults) is caught by the Gerbicz check; the engine rolls back and the
+    returned residue is exact."""
+    k, n = 999, 32768
+    N = _N(k, n)
+    with pg.Engine(k, n) as e:
+        e.set_gerbicz(100, 3)
+        e.set_residue(3)
+        e.square(when)
+        e.debug_corrupt(777, 5)
+        e.square(600 - when)
+        assert e.get_residue() == pow(3, 1 << 600, N)
+        assert e.stats()["gerbicz_failures"] >= 1
+
+
+def test_gerbicz_partial_block_corruption(pg):
+    k, n = 999, 32768
+    N = _N(k, n)
+    with pg.Engine(k, n) as e:
+        e.set_gerbicz(1000, 0)
+        e.set_residue(3)
+        e.square(120)
+        e.debug_corrupt(5, -3)
+        e.square(10)
+        assert e.get_residue() == pow(3, 1 << 130, N)
+        assert e.stats()["gerbicz_failures"] >= 1
+
+
+def test_no_gerbicz_flag_skips_checks(pg):
+    k, n = 999, 32768
+    with pg.Engine(k, n, flags=pg.FLAG_NO_GERBICZ) as e:
+        e.set_residue(3)
+        e.square(300)
+        assert e.get_residue() == pow(3, 1 << 300, _N(k, n))
+        assert e.stats()["gerbicz_checks"] == 0
+
+
+def test_reference_api_shim_is_a_drop_in(pg, gmp, golden):
+    """A caller written only against the reference's fft_init / fft_square_karatsuba /
+    fft_destroy (prothlogic4.2/fft_engine.h) reproduces the reference's RES64 trace."""
+    import subprocess
+    from prothlogic_gb300 import build as b
+    drv = b.COMPAT_DRIVER
+    assert os.path.exists(drv)
+    for t in golden["traces"]:
+        if t["n"] not in (32768, 65536):
+            continue
+        N = _N(t["k"], t["n"])
+        x0 = gmp.powmod(t["a"], t["k"], N)
+        steps = 60
+        out = subprocess.run([drv, str(t["k"]), str(t["n"]), str(t["L"]), str(steps)], input=format(x0, "x"),
+                             capture_output=True, text=True, check=True).stdout.split("\n")
+        got = [ln.split()[1] for ln in out if ln.strip()]
+        assert got == t["res64"][:steps], (t["k"], t["n"])
