@@ -39,6 +39,7 @@ extern "C" {
 #define PG_FLAG_NO_BUMP 0x2u      /* report PG_EROUNDOFF instead of growing the FFT */
 #define PG_FLAG_NO_GRAPH 0x4u     /* launch kernels directly instead of replaying a CUDA graph */
 #define PG_FLAG_FORCE_LEN 0x8u    /* use fft_len_hint exactly, even below the safe length (tests) */
+#define PG_FLAG_NO_PERSIST 0x10u  /* per-pass kernels instead of the persistent cooperative kernel */
 
 typedef struct pg_engine pg_engine;
 typedef struct pg_batch pg_batch;

@@ -23,6 +23,7 @@ FLAG_NO_GERBICZ = 0x1
 FLAG_NO_BUMP = 0x2
 FLAG_NO_GRAPH = 0x4
 FLAG_FORCE_LEN = 0x8
+FLAG_NO_PERSIST = 0x10
 
 _u64 = ctypes.c_uint64
 _u32 = ctypes.c_uint32

@@ -12,6 +12,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -253,17 +254,42 @@ struct Pool {
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (base, count) -> GSTEPS-step graph
     bool big = false;
     bool capturing = false;
+    GridBar* bar = nullptr;      // grid barrier of the persistent kernel
+    int persist_grid = 0;        // co-resident CTAs for it (0: not available)
 };
 
 static const int GSTEPS = 50;  // steps per captured graph
 
+// Launch with programmatic dependent launch: the kernel's prologue (constant
+// loads) overlaps the previous kernel's tail; it waits in griddepcontrol.wait.
+static bool g_use_pdl = true;
+
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+    if (!g_use_pdl) {
+        kern<<<grid, block, 0, s>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 template <int F0>
 static void launch_first(dim3 g, cudaStream_t s, const Slot* sl, int base, const PlanDev& pd) {
-    k_first<F0><<<g, 2 * F0, 0, s>>>(sl, base, pd);
+    launch_pdl(k_first<F0>, g, dim3(2 * F0), s, sl, base, pd);
 }
 template <int F0>
 static void launch_last(dim3 g, cudaStream_t s, const Slot* sl, int base, const PlanDev& pd) {
-    k_last<F0><<<g, 2 * F0, 0, s>>>(sl, base, pd);
+    launch_pdl(k_last<F0>, g, dim3(2 * F0), s, sl, base, pd);
 }
 
 static int enqueue_step_part(Pool* p, int part, int base, int count);
@@ -305,7 +331,7 @@ static int enqueue_step_part(Pool* p, int part, int base, int count) {
     } else if ((d.P == 3 && part == 2) || (d.P == 2 && part == 1)) {
         const dim3 gi(d.M / (Fl * Gi), count);
 #define PG_INNER2(FF, GG, LP) \
-    if (Fl == FF && Gi == GG && d.P - 1 == LP && ++nl) k_inner<FF, GG, LP><<<gi, FF * GG / 4, 0, p->stream>>>(p->dslots, base, d);
+    if (Fl == FF && Gi == GG && d.P - 1 == LP && ++nl) launch_pdl(k_inner<FF, GG, LP>, gi, dim3(FF * GG / 4), p->stream, (const Slot*)p->dslots, base, d);
         PG_INNER2(16, 8, 1) PG_INNER2(32, 4, 1) PG_INNER2(32, 8, 1) PG_INNER2(64, 2, 1) PG_INNER2(64, 8, 1)
         PG_INNER2(128, 2, 1) PG_INNER2(128, 4, 1)
         PG_INNER2(32, 4, 2) PG_INNER2(32, 8, 2) PG_INNER2(64, 2, 2) PG_INNER2(64, 8, 2)
@@ -315,8 +341,8 @@ static int enqueue_step_part(Pool* p, int part, int base, int count) {
         const dim3 gm(d.M / (d.F[1] * Gm), count);
 #define PG_MID2(FF, GG)                                                                            \
     if (d.F[1] == FF && Gm == GG && ++nl) {                                                       \
-        if (part == 1) k_mid_fwd<FF, GG><<<gm, FF * GG / 4, 0, p->stream>>>(p->dslots, base, d);  \
-        else k_mid_inv<FF, GG><<<gm, FF * GG / 4, 0, p->stream>>>(p->dslots, base, d);            \
+        if (part == 1) launch_pdl(k_mid_fwd<FF, GG>, gm, dim3(FF * GG / 4), p->stream, (const Slot*)p->dslots, base, d); \
+        else launch_pdl(k_mid_inv<FF, GG>, gm, dim3(FF * GG / 4), p->stream, (const Slot*)p->dslots, base, d);         \
     }
         PG_MID2(32, 2) PG_MID2(32, 8) PG_MID2(64, 2) PG_MID2(64, 8)
 #undef PG_MID2
@@ -330,6 +356,7 @@ static int enqueue_step_part(Pool* p, int part, int base, int count) {
 static void pool_free(Pool* p) {
     if (!p) return;
     for (auto& kv : p->graphs) cudaGraphExecDestroy(kv.second);
+    cudaFree(p->bar);
     for (int s = 0; s < p->S; ++s)
         if (p->slot_n[s]) put_weights(p->slot_n[s], p->M);
     cudaFree(p->digits);
@@ -463,6 +490,61 @@ static Limbs slot_value(Pool* p, int s) {
     return from_mont(y, sl.k, sl.n);
 }
 
+// ---- persistent (cooperative) path for the three-pass plans ----
+
+static const int kPersistWarps = 8;
+
+typedef void (*PersistFn)(const Slot*, int, int, const PlanDev, long long, GridBar*);
+
+static PersistFn persist_fn(const PlanDev& d) {
+    if (d.P != 3) return nullptr;
+    if (d.F[0] == 16 && d.F[1] == 64 && d.F[2] == 64) return k_persist<16, 64, 64, 2, 2, kPersistWarps>;
+    if (d.F[0] == 32 && d.F[1] == 64 && d.F[2] == 64) return k_persist<32, 64, 64, 2, 2, kPersistWarps>;
+    if (d.F[0] == 32 && d.F[1] == 32 && d.F[2] == 32) return k_persist<32, 32, 32, 4, 4, kPersistWarps>;
+    return nullptr;
+}
+
+// Co-resident grid size for the persistent kernel (0 when unavailable).
+static int persist_prepare(Pool* p) {
+    if (p->persist_grid) return p->persist_grid;
+    PersistFn fn = persist_fn(p->plan->dev);
+    if (!fn) return 0;
+    int dev = 0, sms = 0, coop = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, 32 * kPersistWarps, 0) !=
+            cudaSuccess ||
+        per_sm < 1)
+        return 0;
+    if (!p->bar) {
+        if (cudaMalloc(&p->bar, sizeof(GridBar)) != cudaSuccess) return 0;
+        cudaMemset(p->bar, 0, sizeof(GridBar));
+    }
+    p->persist_grid = sms;  // one CTA per SM: fewer barrier arrivals
+    return p->persist_grid;
+}
+
+// `steps` squarings of slots [base, base+count) in one cooperative launch.
+// Returns PG_ETIMEOUT when a grid barrier gave up (the caller restores state).
+static int pool_run_persist(Pool* p, long long steps, int base, int count) {
+    const int grid = persist_prepare(p);
+    if (!grid) return PG_EINVAL;
+    PersistFn fn = persist_fn(p->plan->dev);
+    PlanDev d = p->plan->dev;
+    const Slot* slots = p->dslots;
+    GridBar* bar = p->bar;
+    void* args[] = {(void*)&slots, (void*)&base, (void*)&count, (void*)&d, (void*)&steps, (void*)&bar};
+    PG_CK(cudaMemsetAsync(p->bar, 0, sizeof(GridBar), p->stream));
+    PG_CK(cudaLaunchCooperativeKernel((const void*)fn, dim3(grid), dim3(32 * kPersistWarps), args, 0, p->stream));
+    g_launches++;
+    GridBar hb;
+    PG_CK(cudaMemcpyAsync(&hb, p->bar, sizeof(GridBar), cudaMemcpyDeviceToHost, p->stream));
+    PG_CK(cudaStreamSynchronize(p->stream));
+    return hb.err ? PG_ETIMEOUT : PG_OK;
+}
+
 // Run `steps` kernel-sequence steps on slots [base, base+count) (graph replay when possible).
 static int pool_run(Pool* p, long long steps, bool use_graph, int base = 0, int count = -1) {
     if (count < 0) count = p->S;
@@ -563,6 +645,7 @@ struct pg_engine {
     uint64_t blocks = 0, in_block = 0;
     uint32_t consecutive_fail = 0;
     bool loaded = false;
+    bool persist = true;  // use the cooperative kernel for plain squaring chains
 };
 
 namespace pg {
@@ -685,7 +768,24 @@ static int run_squarings(pg_engine* e, int s, uint64_t steps) {
         st.partner = s;
         rc = slot_write(e, s, st);
         if (rc) return rc;
-        rc = pool_run(e->pool, (long long)c, !(e->flags & PG_FLAG_NO_GRAPH), s, 1);
+        if (e->persist && persist_prepare(e->pool)) {
+            rc = pool_run_persist(e->pool, (long long)c, s, 1);
+            if (rc == PG_ETIMEOUT) {
+                // a barrier wait ran out: restore the chunk and stay on the per-pass kernels
+                e->persist = false;
+                rc = slot_snapshot(e, s, true);
+                if (rc) return rc;
+                PG_CK(cudaStreamSynchronize(e->pool->stream));
+                continue;
+            }
+            if (!rc) {
+                // the persistent kernel does not touch `active`; keep the state coherent
+                SlotState tmp;
+                rc = slot_state(e, s, &tmp);
+            }
+        } else {
+            rc = pool_run(e->pool, (long long)c, !(e->flags & PG_FLAG_NO_GRAPH), s, 1);
+        }
         if (rc) return rc;
         SlotState after;
         rc = slot_state(e, s, &after);
@@ -906,7 +1006,11 @@ const char* pg_strerror(int s) {
     }
 }
 
-int pg_version(void) { return 100; }
+int pg_version(void) {
+    const char* e = getenv("PROTH_NO_PDL");
+    if (e && *e == '1') g_use_pdl = false;
+    return 100;
+}
 
 int pg_device_info(char* name, size_t name_len, int* sm_count) {
     cudaDeviceProp prop;
@@ -962,6 +1066,7 @@ int pg_create(uint64_t k, uint32_t n, uint32_t fft_len_hint, uint32_t flags, pg_
     e->n = n;
     e->flags = flags;
     e->gz = !(flags & PG_FLAG_NO_GERBICZ);
+    e->persist = !(flags & PG_FLAG_NO_PERSIST);
     e->nslots = e->gz ? NSLOTS_GZ : 1;
     int rc = engine_alloc(e, lg);
     if (rc) {
@@ -1114,7 +1219,10 @@ int pg_time_squarings(pg_engine* e, uint64_t iters, double* ms, uint32_t* kernel
     PG_CK(cudaEventCreate(&a));
     PG_CK(cudaEventCreate(&b));
     PG_CK(cudaEventRecord(a, e->pool->stream));
-    rc = pool_run(e->pool, (long long)iters, !(e->flags & PG_FLAG_NO_GRAPH), SX, 1);
+    if (e->persist && persist_prepare(e->pool))
+        rc = pool_run_persist(e->pool, (long long)iters, SX, 1);
+    else
+        rc = pool_run(e->pool, (long long)iters, !(e->flags & PG_FLAG_NO_GRAPH), SX, 1);
     PG_CK(cudaEventRecord(b, e->pool->stream));
     PG_CK(cudaEventSynchronize(b));
     float f = 0.f;

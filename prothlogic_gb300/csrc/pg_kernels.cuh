@@ -66,6 +66,48 @@ struct Lg { static constexpr int v = (F <= 1) ? 0 : 1 + Lg<F / 2>::v; };
 template <>
 struct Lg<1> { static constexpr int v = 0; };
 
+// Synchronisation policies: a whole CTA, or one warp working on its own tile.
+struct BlockSync {
+    __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct WarpSync {
+    __device__ __forceinline__ void operator()() const { __syncwarp(); }
+};
+
+// Called by a tile after it has loaded its constant operands (twiddles,
+// weights) and before it touches anything the previous kernel wrote.
+// It returns false when the tile has nothing to do (CTA-uniform).
+struct NoWait {
+    __device__ __forceinline__ bool operator()() const { return true; }
+};
+// Programmatic dependent launch: let the next kernel in the stream start its
+// own prologue now, then wait until this kernel's predecessor has completed.
+__device__ __forceinline__ void pdl_wait() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+// ... then go on only if the slot is active in this step (and, for the
+// inverse passes, computes a product of its own).
+struct PdlActive {
+    const SlotState* st;
+    bool need_product;
+    __device__ __forceinline__ bool operator()() const {
+        pdl_wait();
+        return st->active && !(need_product && st->op == OP_FORWARD);
+    }
+};
+// The first pass decides the step's activity from the counters and publishes it.
+struct PdlFirst {
+    SlotState* st;
+    bool publish;
+    __device__ __forceinline__ bool operator()() const {
+        pdl_wait();
+        const bool act = st->step < st->total;
+        if (publish) st->active = act ? 1 : 0;
+        return act;
+    }
+};
+
 // Element (group g, index i) of a shared-memory tile.
 template <int F, int G, bool GROUP_MAJOR>
 __device__ __forceinline__ int tix(int g, int i) {
@@ -76,15 +118,15 @@ __device__ __forceinline__ int tix(int g, int i) {
 // Radix-4 stages with spans F/4, F/16, ...; a final radix-2 stage if log2 F is
 // odd.  Output order is the digit reversal that the host's permutation table
 // (plan construction) describes; the inverse below undoes it exactly.
-template <int F, int G, int NT, bool GM>
-__device__ __forceinline__ void smem_fft_fwd(double2* tile, const double2* __restrict__ wF) {
+template <int F, int G, int NT, bool GM, class Sync>
+__device__ __forceinline__ void smem_fft_fwd(double2* tile, const double2* __restrict__ wF, int tid, Sync sync) {
     constexpr int LG = Lg<F>::v;
     constexpr int N4 = LG / 2;
 #pragma unroll
     for (int s = 0; s < N4; ++s) {
         const int h = F >> (2 * (s + 1));
         const int step = F / (4 * h);
-        for (int b = threadIdx.x; b < G * F / 4; b += NT) {
+        for (int b = tid; b < G * F / 4; b += NT) {
             const int g = b / (F / 4), w = b % (F / 4);
             const int blk = w / h, j = w % h;
             const int i0 = blk * 4 * h + j;
@@ -104,40 +146,40 @@ __device__ __forceinline__ void smem_fft_fwd(double2* tile, const double2* __res
             tile[tix<F, G, GM>(g, i0 + 2 * h)] = a2;
             tile[tix<F, G, GM>(g, i0 + 3 * h)] = a3;
         }
-        __syncthreads();
+        sync();
     }
     if (LG & 1) {
-        for (int b = threadIdx.x; b < G * F / 2; b += NT) {
+        for (int b = tid; b < G * F / 2; b += NT) {
             const int g = b / (F / 2), i0 = 2 * (b % (F / 2));
             const double2 a = tile[tix<F, G, GM>(g, i0)];
             const double2 c = tile[tix<F, G, GM>(g, i0 + 1)];
             tile[tix<F, G, GM>(g, i0)] = make_double2(a.x + c.x, a.y + c.y);
             tile[tix<F, G, GM>(g, i0 + 1)] = make_double2(a.x - c.x, a.y - c.y);
         }
-        __syncthreads();
+        sync();
     }
 }
 
 // Exact inverse (times F) of smem_fft_fwd.
-template <int F, int G, int NT, bool GM>
-__device__ __forceinline__ void smem_fft_inv(double2* tile, const double2* __restrict__ wF) {
+template <int F, int G, int NT, bool GM, class Sync>
+__device__ __forceinline__ void smem_fft_inv(double2* tile, const double2* __restrict__ wF, int tid, Sync sync) {
     constexpr int LG = Lg<F>::v;
     constexpr int N4 = LG / 2;
     if (LG & 1) {
-        for (int b = threadIdx.x; b < G * F / 2; b += NT) {
+        for (int b = tid; b < G * F / 2; b += NT) {
             const int g = b / (F / 2), i0 = 2 * (b % (F / 2));
             const double2 a = tile[tix<F, G, GM>(g, i0)];
             const double2 c = tile[tix<F, G, GM>(g, i0 + 1)];
             tile[tix<F, G, GM>(g, i0)] = make_double2(a.x + c.x, a.y + c.y);
             tile[tix<F, G, GM>(g, i0 + 1)] = make_double2(a.x - c.x, a.y - c.y);
         }
-        __syncthreads();
+        sync();
     }
 #pragma unroll
     for (int s = N4 - 1; s >= 0; --s) {
         const int h = F >> (2 * (s + 1));
         const int step = F / (4 * h);
-        for (int b = threadIdx.x; b < G * F / 4; b += NT) {
+        for (int b = tid; b < G * F / 4; b += NT) {
             const int g = b / (F / 4), w = b % (F / 4);
             const int blk = w / h, j = w % h;
             const int i0 = blk * 4 * h + j;
@@ -157,7 +199,7 @@ __device__ __forceinline__ void smem_fft_inv(double2* tile, const double2* __res
             tile[tix<F, G, GM>(g, i0 + 2 * h)] = z2;
             tile[tix<F, G, GM>(g, i0 + 3 * h)] = z3;
         }
-        __syncthreads();
+        sync();
     }
 }
 
@@ -272,23 +314,33 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 }
 
 // ---------------------------------------------------------------------------
-// k_first: pass 0 forward.  CTA = RUN consecutive columns r (so each row of
-// the tile is one carry run) x F0 rows q; grid (S0 / RUN, slots).
-template <int F0>
-__global__ void __launch_bounds__(2 * F0) k_first(const Slot* __restrict__ slots, int base, const PlanDev pl) {
-    constexpr int G = RUN, NT = 2 * F0;
-    __shared__ double2 tile[F0 * G];
-    __shared__ int dsm[F0 * G];
-    const Slot sl = slots[base + blockIdx.y];
+// Tile functions: NT threads (tid in [0, NT)) process one tile of one slot.
+// The per-pass kernels run one tile per CTA (BlockSync); the persistent kernel
+// runs one tile per warp (WarpSync, NT = 32).
+
+// Pass 0 forward.  Tile = RUN consecutive columns r (each row of the tile is
+// one carry run) x F0 rows q.  Needs NT >= F0.
+template <int F0, int NT, class Sync, class Pre>
+__device__ __forceinline__ void tile_first(const Slot& sl, const PlanDev& pl, int cta, int tid, double2* tile,
+                                           int* dsm, Sync sync, Pre pre) {
+    constexpr int G = RUN;
+    constexpr int PER = (F0 * G + NT - 1) / NT;
     SlotState* st = sl.st;
-    const long long step = st->step;
-    const bool act = step < st->total;
-    if (blockIdx.x == 0 && threadIdx.x == 0) st->active = act ? 1 : 0;
-    if (!act) return;
     const int S0 = pl.S[0];
-    const int r0 = blockIdx.x * G;
+    const int r0 = cta * G;
     const long long nruns = pl.M / RUN;
-    const int tid = threadIdx.x;
+    const double2* __restrict__ tw = pl.tw[0];
+    double2 cw[PER], ct[PER];  // constants, loaded before waiting on the previous kernel
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F0 * G) {
+            const int q = e / G, t = e % G;
+            cw[i] = sl.wf[r0 + t + q * S0];
+            ct[i] = tw[q * S0 + r0 + t];
+        }
+    }
+    if (!pre()) return;
     if (tid < F0) {
         const unsigned long long j0 = (unsigned long long)r0 + (unsigned long long)tid * S0;
         const long long run = (long long)(j0 / RUN);
@@ -314,157 +366,163 @@ __global__ void __launch_bounds__(2 * F0) k_first(const Slot* __restrict__ slots
 #pragma unroll
         for (int t = 0; t < RUN; ++t) dsm[tid * G + t] = dv[t];
     }
-    __syncthreads();
-    for (int e = tid; e < F0 * G; e += NT) {
-        const int q = e / G, t = e % G;
-        const double2 w = sl.wf[r0 + t + q * S0];
-        const double d = (double)dsm[e];
-        tile[e] = make_double2(d * w.x, d * w.y);
+    sync();
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F0 * G) {
+            const double d = (double)dsm[e];
+            tile[e] = make_double2(d * cw[i].x, d * cw[i].y);
+        }
     }
-    __syncthreads();
-    smem_fft_fwd<F0, G, NT, false>(tile, pl.wF[0]);
-    const double2* __restrict__ tw = pl.tw[0];
-    for (int e = tid; e < F0 * G; e += NT) {
-        const int p = e / G, t = e % G;
-        const int r = r0 + t;
-        sl.spec[r + p * S0] = cmul(tile[e], tw[p * S0 + r]);
+    sync();
+    smem_fft_fwd<F0, G, NT, false>(tile, pl.wF[0], tid, sync);
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F0 * G) {
+            const int p = e / G, t = e % G;
+            sl.spec[r0 + t + p * S0] = cmul(tile[e], ct[i]);
+        }
     }
 }
 
-// k_mid_fwd / k_mid_inv: pass 1 of a three-pass plan.  CTA = G consecutive
-// columns of one block of length Mi[1]; grid (M / (F G), slots).
-template <int F, int G>
-__global__ void __launch_bounds__(F * G / 4) k_mid_fwd(const Slot* __restrict__ slots, int base, const PlanDev pl) {
-    constexpr int NT = F * G / 4;
-    __shared__ double2 tile[F * G];
-    const Slot sl = slots[base + blockIdx.y];
-    if (!sl.st->active) return;
+// Pass 1 (three-pass plans).  Tile = G consecutive columns of one block of length Mi[1].
+template <int F, int G, int NT, class Sync, class Pre>
+__device__ __forceinline__ void tile_mid_fwd(const Slot& sl, const PlanDev& pl, int cta, int tid, double2* tile,
+                                             Sync sync, Pre pre) {
+    constexpr int PER = (F * G + NT - 1) / NT;
     const int S = pl.S[1], Mi = pl.Mi[1];
     const int cpb = S / G;
-    const int blk = blockIdx.x / cpb, r0 = (blockIdx.x % cpb) * G;
+    const int blk = cta / cpb, r0 = (cta % cpb) * G;
     double2* bp = sl.spec + (size_t)blk * Mi;
-    const int tid = threadIdx.x;
+    const double2* __restrict__ tw = pl.tw[1];
+    double2 ct[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F * G) ct[i] = tw[(e / G) * S + r0 + e % G];
+    }
+    if (!pre()) return;
     for (int e = tid; e < F * G; e += NT) {
         const int q = e / G, t = e % G;
         tile[e] = bp[r0 + t + q * S];
     }
-    __syncthreads();
-    smem_fft_fwd<F, G, NT, false>(tile, pl.wF[1]);
-    const double2* __restrict__ tw = pl.tw[1];
-    for (int e = tid; e < F * G; e += NT) {
-        const int p = e / G, t = e % G;
-        const int r = r0 + t;
-        bp[r + p * S] = cmul(tile[e], tw[p * S + r]);
+    sync();
+    smem_fft_fwd<F, G, NT, false>(tile, pl.wF[1], tid, sync);
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F * G) bp[r0 + e % G + (e / G) * S] = cmul(tile[e], ct[i]);
     }
 }
 
-template <int F, int G>
-__global__ void __launch_bounds__(F * G / 4) k_mid_inv(const Slot* __restrict__ slots, int base, const PlanDev pl) {
-    constexpr int NT = F * G / 4;
-    __shared__ double2 tile[F * G];
-    const Slot sl = slots[base + blockIdx.y];
-    if (!sl.st->active || sl.st->op == OP_FORWARD) return;
+template <int F, int G, int NT, class Sync, class Pre>
+__device__ __forceinline__ void tile_mid_inv(const Slot& sl, const PlanDev& pl, int cta, int tid, double2* tile,
+                                             Sync sync, Pre pre) {
+    constexpr int PER = (F * G + NT - 1) / NT;
     const int S = pl.S[1], Mi = pl.Mi[1];
     const int cpb = S / G;
-    const int blk = blockIdx.x / cpb, r0 = (blockIdx.x % cpb) * G;
+    const int blk = cta / cpb, r0 = (cta % cpb) * G;
     double2* bp = sl.spec + (size_t)blk * Mi;
     const double2* __restrict__ tw = pl.tw[1];
-    const int tid = threadIdx.x;
-    for (int e = tid; e < F * G; e += NT) {
-        const int p = e / G, t = e % G;
-        const int r = r0 + t;
-        tile[e] = cmulc(bp[r + p * S], tw[p * S + r]);
+    double2 ct[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F * G) ct[i] = tw[(e / G) * S + r0 + e % G];
     }
-    __syncthreads();
-    smem_fft_inv<F, G, NT, false>(tile, pl.wF[1]);
+    if (!pre()) return;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F * G) tile[e] = cmulc(bp[r0 + e % G + (e / G) * S], ct[i]);
+    }
+    sync();
+    smem_fft_inv<F, G, NT, false>(tile, pl.wF[1], tid, sync);
     for (int e = tid; e < F * G; e += NT) {
         const int q = e / G, t = e % G;
         bp[r0 + t + q * S] = tile[e];
     }
 }
 
-// k_inner: last pass.  CTA = G contiguous groups of F: forward, pointwise
-// product with the partner slot's spectrum (itself for a square), inverse.
-template <int F, int G, int LASTP>
-__global__ void __launch_bounds__(F * G / 4) k_inner(const Slot* __restrict__ slots, int base, const PlanDev pl) {
-    constexpr int NT = F * G / 4;
-    __shared__ double2 tile[F * G];
-    __shared__ double2 tile2[F * G];
-    const Slot sl = slots[base + blockIdx.y];
-    SlotState* st = sl.st;
-    if (!st->active) return;
-    const int tid = threadIdx.x;
-    if (blockIdx.x == 0 && tid == 0) st->step += 1;  // nobody reads step until k_last
-    if (st->op == OP_FORWARD) return;                // the partner's k_inner transforms this slot
-    const int partner = st->partner;
-    const bool square = partner == base + (int)blockIdx.y;
-    double2* bp = sl.spec + (size_t)blockIdx.x * (F * G);
-    const double2* qp = slots[partner].spec + (size_t)blockIdx.x * (F * G);
+// Last pass: G contiguous groups of F; forward, pointwise product with the
+// partner's spectrum (itself for a square), inverse.
+template <int F, int G, int LASTP, int NT, class Sync, class Pre>
+__device__ __forceinline__ void tile_inner(const Slot& sl, const Slot& pb, bool square, const PlanDev& pl, int cta,
+                                           int tid, double2* tile, double2* tile2, Sync sync, Pre pre) {
+    if (!pre()) return;
+    double2* bp = sl.spec + (size_t)cta * (F * G);
     for (int e = tid; e < F * G; e += NT) tile[e] = bp[e];
-    if (!square)
+    if (!square) {
+        const double2* qp = pb.spec + (size_t)cta * (F * G);
         for (int e = tid; e < F * G; e += NT) tile2[e] = qp[e];
-    __syncthreads();
-    smem_fft_fwd<F, G, NT, true>(tile, pl.wF[LASTP]);
+    }
+    sync();
+    smem_fft_fwd<F, G, NT, true>(tile, pl.wF[LASTP], tid, sync);
     if (square) {
         for (int e = tid; e < F * G; e += NT) {
             const double2 z = tile[e];
             tile[e] = make_double2(fma(z.x, z.x, -(z.y * z.y)), (z.x + z.x) * z.y);
         }
     } else {
-        smem_fft_fwd<F, G, NT, true>(tile2, pl.wF[LASTP]);
+        smem_fft_fwd<F, G, NT, true>(tile2, pl.wF[LASTP], tid, sync);
         for (int e = tid; e < F * G; e += NT) tile[e] = cmul(tile[e], tile2[e]);
     }
-    __syncthreads();
-    smem_fft_inv<F, G, NT, true>(tile, pl.wF[LASTP]);
+    sync();
+    smem_fft_inv<F, G, NT, true>(tile, pl.wF[LASTP], tid, sync);
     for (int e = tid; e < F * G; e += NT) bp[e] = tile[e];
 }
 
-// k_last: pass 0 inverse + unweight + round + fold + carry within each run.
-template <int F0>
-__global__ void __launch_bounds__(2 * F0) k_last(const Slot* __restrict__ slots, int base, const PlanDev pl) {
-    constexpr int G = RUN, NT = 2 * F0;
-    __shared__ double2 tile[F0 * G];
-    __shared__ long long cl[F0 * G];
-    __shared__ long long ch[F0 * G];
-    __shared__ unsigned long long wmax[NT / 32];
-    const Slot sl = slots[base + blockIdx.y];
+// Pass 0 inverse + unweight + round (max |err|) + Montgomery fold + in-run carry.
+template <int F0, int NT, class Sync, class Pre>
+__device__ __forceinline__ void tile_last(const Slot& sl, const Slot& pb, const PlanDev& pl, int cta, int tid,
+                                          double2* tile, long long* cl, long long* ch, Sync sync, Pre pre) {
+    constexpr int G = RUN;
+    constexpr int PER = (F0 * G + NT - 1) / NT;
     SlotState* st = sl.st;
-    if (!st->active || st->op == OP_FORWARD) return;
     const int S0 = pl.S[0];
-    const int r0 = blockIdx.x * G;
-    const int tid = threadIdx.x;
+    const int r0 = cta * G;
     const double2* __restrict__ tw = pl.tw[0];
-    for (int e = tid; e < F0 * G; e += NT) {
-        const int p = e / G, t = e % G;
-        const int r = r0 + t;
-        tile[e] = cmulc(sl.spec[r + p * S0], tw[p * S0 + r]);
+    double2 ct[PER], cw[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F0 * G) {
+            const int q = e / G, t = e % G;
+            ct[i] = tw[q * S0 + r0 + t];
+            cw[i] = sl.wi[r0 + t + q * S0];
+        }
     }
-    __syncthreads();
-    smem_fft_inv<F0, G, NT, false>(tile, pl.wF[0]);
+    if (!pre()) return;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F0 * G) tile[e] = cmulc(sl.spec[r0 + e % G + (e / G) * S0], ct[i]);
+    }
+    sync();
+    smem_fft_inv<F0, G, NT, false>(tile, pl.wF[0], tid, sync);
     unsigned long long emax = 0;
     int badr = 0;
-    for (int e = tid; e < F0 * G; e += NT) {
-        const int q = e / G, t = e % G;
-        const double2 z = cmul(tile[e], sl.wi[r0 + t + q * S0]);
-        cl[e] = round_track(z.x, emax, badr);
-        ch[e] = round_track(z.y, emax, badr);
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F0 * G) {
+            const double2 z = cmul(tile[e], cw[i]);
+            cl[e] = round_track(z.x, emax, badr);
+            ch[e] = round_track(z.y, emax, badr);
+        }
     }
     if (badr) {
         emax = (unsigned long long)__double_as_longlong(1.0);
         atomicOr(&st->flags, SF_ROUND_RANGE);
     }
     emax = warp_max_u64(emax);
-    if ((tid & 31) == 0) wmax[tid >> 5] = emax;
-    __syncthreads();
-    if (tid == 0) {
-        unsigned long long m = 0;
-        for (int w = 0; w < NT / 32; ++w) m = wmax[w] > m ? wmax[w] : m;
-        atomicMax(&st->maxerr_bits, m);
-    }
+    if ((tid & 31) == 0 && emax > 0) atomicMax(&st->maxerr_bits, emax);
+    sync();
     if (tid < F0) {
         const unsigned long long j0 = (unsigned long long)r0 + (unsigned long long)tid * S0;
         const long long run = (long long)(j0 / RUN);
-        const Slot& pb = slots[st->partner];
         int4* dp = reinterpret_cast<int4*>(sl.digits + j0);
         const int4* qp = reinterpret_cast<const int4*>(pb.digits + j0);
         const int4 v0 = dp[0], v1 = dp[1], w0 = qp[0], w1 = qp[1];
@@ -487,6 +545,158 @@ __global__ void __launch_bounds__(2 * F0) k_last(const Slot* __restrict__ slots,
         dp[0] = make_int4(nd[0], nd[1], nd[2], nd[3]);
         dp[1] = make_int4(nd[4], nd[5], nd[6], nd[7]);
         store_carry(sl.carries, run, carry);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-pass kernels: one tile per CTA, blockIdx.y = slot - base.
+
+template <int F0>
+__global__ void __launch_bounds__(2 * F0) k_first(const Slot* __restrict__ slots, int base, const PlanDev pl) {
+    __shared__ double2 tile[F0 * RUN];
+    __shared__ int dsm[F0 * RUN];
+    const Slot sl = slots[base + blockIdx.y];
+    tile_first<F0, 2 * F0>(sl, pl, blockIdx.x, threadIdx.x, tile, dsm, BlockSync(),
+                           PdlFirst{sl.st, blockIdx.x == 0 && threadIdx.x == 0});
+}
+
+template <int F, int G>
+__global__ void __launch_bounds__(F * G / 4) k_mid_fwd(const Slot* __restrict__ slots, int base, const PlanDev pl) {
+    __shared__ double2 tile[F * G];
+    const Slot sl = slots[base + blockIdx.y];
+    tile_mid_fwd<F, G, F * G / 4>(sl, pl, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlActive{sl.st, false});
+}
+
+template <int F, int G>
+__global__ void __launch_bounds__(F * G / 4) k_mid_inv(const Slot* __restrict__ slots, int base, const PlanDev pl) {
+    __shared__ double2 tile[F * G];
+    const Slot sl = slots[base + blockIdx.y];
+    tile_mid_inv<F, G, F * G / 4>(sl, pl, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlActive{sl.st, true});
+}
+
+template <int F, int G, int LASTP>
+__global__ void __launch_bounds__(F * G / 4) k_inner(const Slot* __restrict__ slots, int base, const PlanDev pl) {
+    __shared__ double2 tile[F * G];
+    __shared__ double2 tile2[F * G];
+    const Slot sl = slots[base + blockIdx.y];
+    SlotState* st = sl.st;
+    pdl_wait();
+    if (!st->active) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->step += 1;  // nobody reads step until k_last
+    if (st->op == OP_FORWARD) return;                       // the partner's k_inner transforms this slot
+    const int partner = st->partner;
+    const bool square = partner == base + (int)blockIdx.y;
+    tile_inner<F, G, LASTP, F * G / 4>(sl, slots[partner], square, pl, blockIdx.x, threadIdx.x, tile, tile2,
+                                        BlockSync(), NoWait());
+}
+
+template <int F0>
+__global__ void __launch_bounds__(2 * F0) k_last(const Slot* __restrict__ slots, int base, const PlanDev pl) {
+    __shared__ double2 tile[F0 * RUN];
+    __shared__ long long cl[F0 * RUN];
+    __shared__ long long ch[F0 * RUN];
+    const Slot sl = slots[base + blockIdx.y];
+    SlotState* st = sl.st;
+    // the partner index is fixed by the host before the step: safe to read early
+    tile_last<F0, 2 * F0>(sl, slots[st->partner], pl, blockIdx.x, threadIdx.x, tile, cl, ch, BlockSync(),
+                          PdlActive{st, true});
+}
+
+// ---------------------------------------------------------------------------
+// Persistent kernel: `steps` squarings of slots [base, base + count) in one
+// cooperative launch, the five passes separated by a grid barrier.  Each warp
+// is a worker that takes tiles w, w + W, ... of a pass (worker ids interleave
+// CTAs, so consecutive tiles land on different SMs).
+
+struct GridBar {
+    unsigned count;
+    unsigned gen;
+    int err;        // set when a barrier wait ran out of its spin budget
+    int pad;
+};
+
+// All CTAs of a cooperative grid meet here.  Every wait is bounded: after
+// kBarSpins polls the CTA records the failure and returns false, and every
+// CTA then leaves the kernel at its next barrier.
+constexpr long long kBarSpins = 1ll << 24;
+
+__device__ __forceinline__ bool grid_barrier(GridBar* bar) {
+    __syncthreads();
+    __shared__ int ok;
+    if (threadIdx.x == 0) {
+        volatile unsigned* vgen = &bar->gen;
+        volatile int* verr = &bar->err;
+        const unsigned g = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(&bar->count, 1u) + 1u;
+        int good = 1;
+        if (arrived == gridDim.x) {
+            bar->count = 0;
+            __threadfence();
+            atomicAdd(&bar->gen, 1u);
+        } else {
+            long long spins = 0;
+            while (*vgen == g) {
+                if (*verr || ++spins > kBarSpins) {
+                    atomicExch(&bar->err, 1);
+                    good = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        ok = good && !*verr;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <int F0, int F1, int F2, int G1, int G2, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_persist(const Slot* __restrict__ slots, int base, int count,
+                                                        const PlanDev pl, long long steps, GridBar* bar) {
+    static_assert(F0 <= 32 && F1 * G1 / 4 >= 32 && F2 * G2 / 4 >= 32, "one warp per tile");
+    constexpr int TILE = (F0 * RUN > F1 * G1 ? (F0 * RUN > F2 * G2 ? F0 * RUN : F2 * G2)
+                                             : (F1 * G1 > F2 * G2 ? F1 * G1 : F2 * G2));
+    __shared__ double2 sm_tile[WARPS][TILE];
+    __shared__ long long sm_i64[WARPS][2 * F0 * RUN];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int W = WARPS * gridDim.x;
+    const int wid = warp * gridDim.x + blockIdx.x;
+    double2* tile = sm_tile[warp];
+    int* dsm = reinterpret_cast<int*>(sm_i64[warp]);
+    long long* cl = sm_i64[warp];
+    long long* ch = sm_i64[warp] + F0 * RUN;
+    const int t_first = (pl.S[0] / RUN), t_mid = pl.M / (F1 * G1), t_inner = pl.M / (F2 * G2);
+    const WarpSync ws;
+    for (long long it = 0; it < steps; ++it) {
+        for (int t = wid; t < t_first * count; t += W) {
+            const int s = base + t / t_first;
+            tile_first<F0, 32>(slots[s], pl, t % t_first, lane, tile, dsm, ws, NoWait());
+        }
+        if (!grid_barrier(bar)) return;
+        for (int t = wid; t < t_mid * count; t += W) {
+            const int s = base + t / t_mid;
+            tile_mid_fwd<F1, G1, 32>(slots[s], pl, t % t_mid, lane, tile, ws, NoWait());
+        }
+        if (!grid_barrier(bar)) return;
+        for (int t = wid; t < t_inner * count; t += W) {
+            const int s = base + t / t_inner;
+            const int c = t % t_inner;
+            if (c == 0 && lane == 0) slots[s].st->step += 1;
+            tile_inner<F2, G2, 2, 32>(slots[s], slots[s], true, pl, c, lane, tile, tile, ws, NoWait());
+        }
+        if (!grid_barrier(bar)) return;
+        for (int t = wid; t < t_mid * count; t += W) {
+            const int s = base + t / t_mid;
+            tile_mid_inv<F1, G1, 32>(slots[s], pl, t % t_mid, lane, tile, ws, NoWait());
+        }
+        if (!grid_barrier(bar)) return;
+        for (int t = wid; t < t_first * count; t += W) {
+            const int s = base + t / t_first;
+            tile_last<F0, 32>(slots[s], slots[s], pl, t % t_first, lane, tile, cl, ch, ws, NoWait());
+        }
+        if (!grid_barrier(bar)) return;
     }
 }
 

@@ -38,11 +38,13 @@ def test_device_is_gb300(pg):
 
 
 @pytest.mark.parametrize("k,n", [(3, 2048), (843, 4096), (9999, 5000), (77, 8300), (524287, 20000),
-                                 (5, 32700), (12345, 65536), (999999, 131072), (3, 270000)])
-def test_steps_match_python(pg, k, n):
+                                 (5, 32700), (12345, 65536), (999999, 131072), (3, 270000), (77, 600000)])
+@pytest.mark.parametrize("path", ["persistent", "per-pass"])
+def test_steps_match_python(pg, k, n, path):
     N = _N(k, n)
     x = random.Random(n * 31 + k).randrange(N)
-    with pg.Engine(k, n, flags=pg.FLAG_NO_GRAPH) as e:
+    flags = pg.FLAG_NO_GRAPH | (pg.FLAG_NO_PERSIST if path == "per-pass" else 0)
+    with pg.Engine(k, n, flags=flags) as e:
         e.set_residue(x)
         assert e.get_residue() == x
         for i in range(10):
@@ -64,6 +66,23 @@ def test_reference_traces(pg, gmp, golden):
                 e.square(1)
                 got = e.get_residue()
                 assert format(got & M64, "016x") == want, (k, n, i)
+
+
+@pytest.mark.parametrize("n", [524288, 1 << 20, 2000000])
+def test_persistent_equals_per_pass_at_full_size(pg, n):
+    """Long chains at the large lengths: the cooperative kernel and the per-pass
+    kernels give identical residues (and equal to Python at the smaller n)."""
+    k = 878261
+    res = []
+    for flags in (0, pg.FLAG_NO_PERSIST):
+        with pg.Engine(k, n, flags=flags | pg.FLAG_NO_GERBICZ) as e:
+            e.set_residue(5)
+            e.square(300)
+            res.append(e.get_residue())
+            assert e.max_err() < 0.4
+    assert res[0] == res[1]
+    if n <= 524288:
+        assert res[0] == pow(5, 1 << 300, _N(k, n))
 
 
 def test_reference_full_tests(pg, golden):
@@ -163,7 +182,7 @@ def test_checkpoint_roundtrip(pg, tmp_path):
 def test_roundoff_bump_recovers(pg):
     """A forced, far too small FFT length overflows the rounding range; the
     engine rolls back, grows the length and still returns the exact residue."""
-    k, n = 999999, 45000  # 22 bits per digit at length 2048: products overflow FP64 rounding
+    k, n = 999999, 49100  # 24 bits per digit at length 2048: products leave FP64's exact range
     N = _N(k, n)
     with pg.Engine(k, n, fft_len_hint=2048, flags=pg.FLAG_FORCE_LEN) as e:
         assert e.fft_len == 2048
@@ -182,7 +201,7 @@ def test_digit_width_limits(pg):
 
 
 def test_roundoff_without_bump_reports(pg):
-    with pg.Engine(999999, 45000, fft_len_hint=2048, flags=pg.FLAG_FORCE_LEN | pg.FLAG_NO_BUMP) as e:
+    with pg.Engine(999999, 49100, fft_len_hint=2048, flags=pg.FLAG_FORCE_LEN | pg.FLAG_NO_BUMP) as e:
         e.set_residue(5)
         with pytest.raises(pg.ProthGpuError) as ei:
             e.square(20)
