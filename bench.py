@@ -223,6 +223,41 @@ def run_reference(args, world, rank, pgd):
     return 0
 
 
+def batched_sample(pg, steps=300, warm=60):
+    """Batched vs one-at-a-time tests/hour at n = 65536 (4096 candidates, k odd in
+    [3, 10^6), seed 3), from a bounded sample of squaring steps on the device."""
+    cands = workloads.uniform(count=4096)
+    n = cands[0][1]
+    b = pg.Batch(4096)
+    admitted = 0
+    for i, (k, nn) in enumerate(cands):
+        b.submit(k, nn, i)
+    b.run_timed(warm)                       # admission + graph capture + warm-up
+    ms = b.run_timed(steps)
+    q, running, fin = b.pending()
+    admitted = running
+    b.close()
+    per_step_ms = ms / steps
+    sq_per_test = n - 1 + 19                # n-1 squarings + the a^k powering (bitlen(k) - 1 <= 19)
+    tph_batch = admitted / (per_step_ms * 1e-3 * sq_per_test) * 3600.0
+    # one candidate at a time on the whole GPU (same engine, FFT length 4096)
+    k0 = cands[0][0]
+    e = pg.Engine(k0, n, flags=pg.FLAG_NO_GERBICZ)
+    e.set_residue(3)
+    e.time_squarings(200)
+    ms1, _ = e.time_squarings(2000)
+    e.close()
+    us1 = ms1 * 1e3 / 2000
+    tph_single = 3600.0 / (us1 * 1e-6 * sq_per_test)
+    return {"workload": "uniform: 4096 candidates, n=65536, k odd in [3,10^6) seed 3",
+            "running_slots": admitted, "batch_step_ms": per_step_ms,
+            "batched_tests_per_hour": tph_batch, "one_at_a_time_tests_per_hour": tph_single,
+            "batched_over_one_at_a_time": tph_batch / tph_single,
+            "one_at_a_time_us_per_squaring": us1,
+            "sample": f"{steps} batch squaring steps after {warm} warm-up; one-at-a-time 2000 squarings; "
+                      "tests/hour extrapolated to n-1+19 squarings per test; no Gerbicz in either"}
+
+
 def run_gpu(args, world, rank, local, pgd):
     import prothlogic_gb300 as pg
     pg.set_device(local)
@@ -257,6 +292,7 @@ def run_gpu(args, world, rank, local, pgd):
     total_ms = max_over_ranks(pgd, sum(step_ms))
     stats = eng.stats()
     res = eng.get_residue()
+    max_err = eng.max_err()
     value = total_ms * 1e6 / (K * SQ_PER_STEP * world)
 
     # parity of the timed run: RES64 after K*1000 squarings of x0 = a (GMP values)
@@ -300,6 +336,8 @@ def run_gpu(args, world, rank, local, pgd):
     if rank != 0:
         eng.close()
         return 0
+    eng.close()
+    batched = batched_sample(pg) if os.environ.get("PROTH_BENCH_BATCH", "1") == "1" else None
     cpu_ns, cpu_kind, cpu_used, cpu_L = time_cpu_reference(k, n, a, cpu_sample_seconds())
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -310,7 +348,7 @@ def run_gpu(args, world, rank, local, pgd):
                    "gerbicz": f"block {SQ_PER_STEP}, {K} blocks verified in the last step",
                    "l2": "flushed between steps (512 MiB write)", "parity_res64": parity,
                    "gerbicz_checks": stats["gerbicz_checks"], "gerbicz_failures": stats["gerbicz_failures"],
-                   "fft_bumps": stats["fft_bumps"], "max_err": eng.max_err()},
+                   "fft_bumps": stats["fft_bumps"], "max_err": max_err},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved_gbs / hbm_peak if hbm_peak else None, "traffic": traffic,
                      "note": "measured hbm_gbs peak; per squaring (the 5 kernels of one squaring); "
@@ -327,9 +365,9 @@ def run_gpu(args, world, rank, local, pgd):
                 "note": "set_residue + 1,000 squarings + verified get_residue per step"},
         "clocks": clocks,
         "gpu_launches": launches,
+        "batched": batched,
     }
     print(json.dumps(line), flush=True)
-    eng.close()
     return 0
 
 

@@ -39,7 +39,8 @@ extern "C" {
 #define PG_FLAG_NO_BUMP 0x2u      /* report PG_EROUNDOFF instead of growing the FFT */
 #define PG_FLAG_NO_GRAPH 0x4u     /* launch kernels directly instead of replaying a CUDA graph */
 #define PG_FLAG_FORCE_LEN 0x8u    /* use fft_len_hint exactly, even below the safe length (tests) */
-#define PG_FLAG_NO_PERSIST 0x10u  /* per-pass kernels instead of the persistent cooperative kernel */
+#define PG_FLAG_NO_PERSIST 0x10u  /* (default) per-pass kernels, not the persistent cooperative kernel */
+#define PG_FLAG_PERSIST 0x20u     /* squaring chains in the persistent cooperative kernel */
 
 typedef struct pg_engine pg_engine;
 typedef struct pg_batch pg_batch;
@@ -154,6 +155,9 @@ int pg_batch_submit(pg_batch* b, uint64_t k, uint32_t n, uint64_t tag);
 /* Advance every admitted candidate by up to `max_steps` squarings (0: until
  * all queued candidates are done), admitting queued ones into free slots. */
 int pg_batch_run(pg_batch* b, uint64_t max_steps);
+/* pg_batch_run bracketed by CUDA events on every FFT-length class's stream;
+ * *ms is the longest class's device time (admission and collection included). */
+int pg_batch_run_timed(pg_batch* b, uint64_t max_steps, double* ms);
 /* Move up to `cap` finished results out; *count receives how many. */
 int pg_batch_poll(pg_batch* b, pg_result* out, size_t cap, size_t* count);
 /* Queued, running and finished-but-unpolled candidate counts. */

@@ -10,6 +10,9 @@
 //       "verdict res64 maxerr".
 //   ref_harness time <k> <n> <L> <steps>
 //       engine-only microseconds per squaring.
+//   ref_harness ckpt_save <k> <n> <L> <current_i> <path>   (hex residue on stdin)
+//       writes a checkpoint with the reference's save_checkpoint (checkpoint_manager.cpp:8-23).
+#include "checkpoint_manager.h"
 #include "fft_engine.h"
 #include "proth_logic.h"
 #include <cctype>
@@ -45,6 +48,14 @@ int main(int argc, char** argv) {
     const size_t nl = L / 4;
     size_t alloc = std::max(L, (size_t)((2 * n) / 64 + 64));
     std::vector<uint64_t> limbs(alloc, 0);
+    if (mode == "ckpt_save") {
+        std::string hex;
+        for (int ch; (ch = getchar()) != EOF;)
+            if (isxdigit(ch)) hex.push_back((char)ch);
+        std::vector<uint64_t> x = parse_hex(hex.c_str(), nl);
+        const uint64_t ci = strtoull(argv[5], nullptr, 10);
+        return save_checkpoint(ci, nl, x.data(), argv[6]) ? 0 : 4;
+    }
     if (mode == "test") {
         bool prime = execute_proth_test_fft(k, n, limbs.data(), ctx, 0);
         printf("%d %016llx %.6g\n", prime ? 1 : 0, (unsigned long long)limbs[0], ctx.last_max_diff);

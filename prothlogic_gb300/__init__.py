@@ -24,6 +24,7 @@ FLAG_NO_BUMP = 0x2
 FLAG_NO_GRAPH = 0x4
 FLAG_FORCE_LEN = 0x8
 FLAG_NO_PERSIST = 0x10
+FLAG_PERSIST = 0x20
 
 _u64 = ctypes.c_uint64
 _u32 = ctypes.c_uint32
@@ -87,6 +88,7 @@ SIGNATURES = {
     "pg_batch_submit": (ctypes.c_int, [_vp, _u64, _u32, _u64]),
     "pg_batch_run": (ctypes.c_int, [_vp, _u64]),
     "pg_batch_poll": (ctypes.c_int, [_vp, ctypes.POINTER(PgResult), _sz, ctypes.POINTER(_sz)]),
+    "pg_batch_run_timed": (ctypes.c_int, [_vp, _u64, ctypes.POINTER(ctypes.c_double)]),
     "pg_batch_pending": (ctypes.c_int, [_vp, ctypes.POINTER(_sz), ctypes.POINTER(_sz), ctypes.POINTER(_sz)]),
 }
 
@@ -288,6 +290,12 @@ class Batch:
 
     def run(self, max_steps=0):
         _check(load().pg_batch_run(self._h, max_steps), "pg_batch_run")
+
+    def run_timed(self, max_steps):
+        """pg_batch_run with CUDA events on the class streams; returns device ms."""
+        ms = ctypes.c_double()
+        _check(load().pg_batch_run_timed(self._h, max_steps, ctypes.byref(ms)), "pg_batch_run_timed")
+        return ms.value
 
     def poll(self, cap=4096):
         arr = (PgResult * cap)()

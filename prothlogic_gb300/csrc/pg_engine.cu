@@ -216,8 +216,11 @@ static void put_weights(unsigned n, unsigned M) {
 }
 
 // Largest bits per digit allowed at each length (roundoff stays well under 0.4).
+// Measured on GB300 (max |err| over 300 squarings of random residues, k = 999999):
+// at 2^8 .. 2^18 the error reaches ~0.05 around 21.5 .. 19 bits per digit; the
+// table stays about half a bit to a bit below that (the 0.4 guard bumps anyway).
 static double max_bits_per_digit(int lg) {
-    static const double t[] = {19.5, 19.5, 19.0, 19.0, 18.5, 18.5, 18.0, 18.0, 17.5, 17.0, 16.5};
+    static const double t[] = {21.0, 20.5, 20.5, 20.0, 20.0, 19.5, 19.0, 18.5, 18.5, 18.0, 17.5};
     return t[std::min(std::max(lg - kMinLg, 0), kMaxLg - kMinLg)];
 }
 
@@ -262,11 +265,17 @@ static const int GSTEPS = 50;  // steps per captured graph
 
 // Launch with programmatic dependent launch: the kernel's prologue (constant
 // loads) overlaps the previous kernel's tail; it waits in griddepcontrol.wait.
-static bool g_use_pdl = true;
+static bool use_pdl() {
+    static const bool on = [] {
+        const char* e = getenv("PROTH_NO_PDL");
+        return !(e && *e == '1');
+    }();
+    return on;
+}
 
 template <typename... KArgs, typename... Args>
 static void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
-    if (!g_use_pdl) {
+    if (!use_pdl()) {
         kern<<<grid, block, 0, s>>>(args...);
         return;
     }
@@ -284,20 +293,20 @@ static void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream
 }
 
 template <int F0>
-static void launch_first(dim3 g, cudaStream_t s, const Slot* sl, int base, const PlanDev& pd) {
-    launch_pdl(k_first<F0>, g, dim3(2 * F0), s, sl, base, pd);
+static void launch_first(dim3 g, cudaStream_t s, const Slot* sl, int base, const PlanDev& pd, const Slot& one) {
+    launch_pdl(k_first<F0>, g, dim3(2 * F0), s, sl, base, pd, one);
 }
 template <int F0>
-static void launch_last(dim3 g, cudaStream_t s, const Slot* sl, int base, const PlanDev& pd) {
-    launch_pdl(k_last<F0>, g, dim3(2 * F0), s, sl, base, pd);
+static void launch_last(dim3 g, cudaStream_t s, const Slot* sl, int base, const PlanDev& pd, const Slot& one) {
+    launch_pdl(k_last<F0>, g, dim3(2 * F0), s, sl, base, pd, one);
 }
 
-static int enqueue_step_part(Pool* p, int part, int base, int count);
+static int enqueue_step_part(Pool* p, int part, int base, int count, bool solo = false);
 
-static int enqueue_step(Pool* p, int base, int count) {
+static int enqueue_step(Pool* p, int base, int count, bool solo = false) {
     const int parts = p->plan->dev.P == 3 ? 5 : 3;
     for (int i = 0; i < parts; ++i) {
-        const int rc = enqueue_step_part(p, i, base, count);
+        const int rc = enqueue_step_part(p, i, base, count, solo);
         if (rc) return rc;
     }
     return PG_OK;
@@ -305,10 +314,15 @@ static int enqueue_step(Pool* p, int base, int count) {
 
 // Launch one kernel of the step sequence: part 0 = first pass, then mid fwd,
 // inner, mid inv (three-pass plans), last pass.  Returns PG_EINVAL past the end.
-static int enqueue_step_part(Pool* p, int part, int base, int count) {
+// solo: one residue squared for exactly the steps the host runs (descriptor by value).
+static int enqueue_step_part(Pool* p, int part, int base, int count, bool solo) {
     const PlanDev& d = p->plan->dev;
     const int parts = d.P == 3 ? 5 : 3;
     if (part < 0 || part >= parts || base < 0 || count < 1 || base + count > p->S) return PG_EINVAL;
+    if (solo && count != 1) return PG_EINVAL;
+    Slot one;
+    memset(&one, 0, sizeof(one));
+    if (solo) one = p->hslots[base];
     const dim3 g0(d.S[0] / RUN, count);
     const int Gm = p->big ? p->plan->Gmid_big : p->plan->Gmid_small;
     const int Gi = p->big ? p->plan->Ginner_big : p->plan->Ginner_small;
@@ -316,22 +330,22 @@ static int enqueue_step_part(Pool* p, int part, int base, int count) {
     int nl = 0;
     if (part == 0) {
         switch (d.F[0]) {
-            case 16: launch_first<16>(g0, p->stream, p->dslots, base, d); break;
-            case 32: launch_first<32>(g0, p->stream, p->dslots, base, d); break;
-            case 64: launch_first<64>(g0, p->stream, p->dslots, base, d); break;
-            case 128: launch_first<128>(g0, p->stream, p->dslots, base, d); break;
+            case 16: launch_first<16>(g0, p->stream, p->dslots, base, d, one); break;
+            case 32: launch_first<32>(g0, p->stream, p->dslots, base, d, one); break;
+            case 64: launch_first<64>(g0, p->stream, p->dslots, base, d, one); break;
+            case 128: launch_first<128>(g0, p->stream, p->dslots, base, d, one); break;
         }
     } else if (part == parts - 1) {
         switch (d.F[0]) {
-            case 16: launch_last<16>(g0, p->stream, p->dslots, base, d); break;
-            case 32: launch_last<32>(g0, p->stream, p->dslots, base, d); break;
-            case 64: launch_last<64>(g0, p->stream, p->dslots, base, d); break;
-            case 128: launch_last<128>(g0, p->stream, p->dslots, base, d); break;
+            case 16: launch_last<16>(g0, p->stream, p->dslots, base, d, one); break;
+            case 32: launch_last<32>(g0, p->stream, p->dslots, base, d, one); break;
+            case 64: launch_last<64>(g0, p->stream, p->dslots, base, d, one); break;
+            case 128: launch_last<128>(g0, p->stream, p->dslots, base, d, one); break;
         }
     } else if ((d.P == 3 && part == 2) || (d.P == 2 && part == 1)) {
         const dim3 gi(d.M / (Fl * Gi), count);
 #define PG_INNER2(FF, GG, LP) \
-    if (Fl == FF && Gi == GG && d.P - 1 == LP && ++nl) launch_pdl(k_inner<FF, GG, LP>, gi, dim3(FF * GG / 4), p->stream, (const Slot*)p->dslots, base, d);
+    if (Fl == FF && Gi == GG && d.P - 1 == LP && ++nl) launch_pdl(k_inner<FF, GG, LP>, gi, dim3(FF * GG / 4), p->stream, (const Slot*)p->dslots, base, d, one);
         PG_INNER2(16, 8, 1) PG_INNER2(32, 4, 1) PG_INNER2(32, 8, 1) PG_INNER2(64, 2, 1) PG_INNER2(64, 8, 1)
         PG_INNER2(128, 2, 1) PG_INNER2(128, 4, 1)
         PG_INNER2(32, 4, 2) PG_INNER2(32, 8, 2) PG_INNER2(64, 2, 2) PG_INNER2(64, 8, 2)
@@ -341,8 +355,8 @@ static int enqueue_step_part(Pool* p, int part, int base, int count) {
         const dim3 gm(d.M / (d.F[1] * Gm), count);
 #define PG_MID2(FF, GG)                                                                            \
     if (d.F[1] == FF && Gm == GG && ++nl) {                                                       \
-        if (part == 1) launch_pdl(k_mid_fwd<FF, GG>, gm, dim3(FF * GG / 4), p->stream, (const Slot*)p->dslots, base, d); \
-        else launch_pdl(k_mid_inv<FF, GG>, gm, dim3(FF * GG / 4), p->stream, (const Slot*)p->dslots, base, d);         \
+        if (part == 1) launch_pdl(k_mid_fwd<FF, GG>, gm, dim3(FF * GG / 4), p->stream, (const Slot*)p->dslots, base, d, one); \
+        else launch_pdl(k_mid_inv<FF, GG>, gm, dim3(FF * GG / 4), p->stream, (const Slot*)p->dslots, base, d, one);         \
     }
         PG_MID2(32, 2) PG_MID2(32, 8) PG_MID2(64, 2) PG_MID2(64, 8)
 #undef PG_MID2
@@ -530,7 +544,7 @@ static int persist_prepare(Pool* p) {
 // Returns PG_ETIMEOUT when a grid barrier gave up (the caller restores state).
 static int pool_run_persist(Pool* p, long long steps, int base, int count) {
     const int grid = persist_prepare(p);
-    if (!grid) return PG_EINVAL;
+    if (!grid || count != 1) return PG_EINVAL;
     PersistFn fn = persist_fn(p->plan->dev);
     PlanDev d = p->plan->dev;
     const Slot* slots = p->dslots;
@@ -546,9 +560,9 @@ static int pool_run_persist(Pool* p, long long steps, int base, int count) {
 }
 
 // Run `steps` kernel-sequence steps on slots [base, base+count) (graph replay when possible).
-static int pool_run(Pool* p, long long steps, bool use_graph, int base = 0, int count = -1) {
+static int pool_run(Pool* p, long long steps, bool use_graph, int base = 0, int count = -1, bool solo = false) {
     if (count < 0) count = p->S;
-    const auto key = std::make_pair(base, count);
+    const auto key = std::make_pair(solo ? -1 - base : base, count);
     cudaGraphExec_t ge = nullptr;
     if (use_graph && steps >= GSTEPS) {
         auto it = p->graphs.find(key);
@@ -559,7 +573,7 @@ static int pool_run(Pool* p, long long steps, bool use_graph, int base = 0, int 
             PG_CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
             int rc = PG_OK;
             p->capturing = true;
-            for (int i = 0; i < GSTEPS && rc == PG_OK; ++i) rc = enqueue_step(p, base, count);
+            for (int i = 0; i < GSTEPS && rc == PG_OK; ++i) rc = enqueue_step(p, base, count, solo);
             p->capturing = false;
             cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
             if (rc) return rc;
@@ -575,7 +589,7 @@ static int pool_run(Pool* p, long long steps, bool use_graph, int base = 0, int 
             g_launches += (unsigned long long)GSTEPS * (p->plan->dev.P == 3 ? 5 : 3);
             steps -= GSTEPS;
         } else {
-            int rc = enqueue_step(p, base, count);
+            int rc = enqueue_step(p, base, count, solo);
             if (rc) return rc;
             steps -= 1;
         }
@@ -608,10 +622,11 @@ __global__ void k_dfma_peak(double* out, int iters, double a, double b) {
 // single-candidate engine
 
 // Slots of a single-candidate engine's pool.  With the Gerbicz check on:
-//   X  the residue          D   product of block-end residues since X0
-//   Y  scratch: the previous D, then the verification value
-//   X0 last verified residue XB residue at the start of the current block
-enum { SX = 0, SD = 1, SY = 2, SX0 = 3, SXB = 4, NSLOTS_GZ = 5 };
+//   X   the residue                 Y   concurrent verification chain (squared beside X)
+//   D   product of block-end residues since X0
+//   X0  last verified residue       XB  residue at the start of the current block
+//   YP  D before the last product (sequential verification at a flush)
+enum { SX = 0, SY = 1, SD = 2, SX0 = 3, SXB = 4, SYP = 5, NSLOTS_GZ = 6 };
 
 __global__ void k_copy_state(const Slot* __restrict__ slots, int src, int dst) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
@@ -644,6 +659,7 @@ struct pg_engine {
     bool armed = false;
     uint64_t blocks = 0, in_block = 0;
     uint32_t consecutive_fail = 0;
+    bool y_live = false;  // Y holds D_{t-1} and is being squared beside X in the current block
     bool loaded = false;
     bool persist = true;  // use the cooperative kernel for plain squaring chains
 };
@@ -749,54 +765,64 @@ static int engine_bump(pg_engine* e) {
     return PG_OK;
 }
 
-// Square slot s `steps` times, chunk by chunk: each chunk is checked for
-// roundoff > 0.4 and digit overflow; a bad chunk is rolled back and redone at
-// the next FFT length.
-static int run_squarings(pg_engine* e, int s, uint64_t steps) {
+// Square slots [s, s + count) `steps` times, chunk by chunk: each chunk is
+// checked for roundoff > 0.4 and digit overflow.  A bad chunk of a single slot
+// is rolled back and redone at the next FFT length; for a pair the caller gets
+// PG_EROUNDOFF after the bump and restarts from its own verified state.
+static int run_squarings(pg_engine* e, int s, uint64_t steps, int count = 1) {
     const uint64_t CHUNK = 2000;
     int guard = 0;
     while (steps > 0) {
         const uint64_t c = std::min<uint64_t>(steps, CHUNK);
-        SlotState st;
-        int rc = slot_state(e, s, &st);
+        int rc = PG_OK;
+        std::vector<SlotState> st(count);
+        for (int i = 0; i < count && !rc; ++i) rc = slot_state(e, s + i, &st[i]);
+        if (!rc && count == 1) rc = slot_snapshot(e, s, false);
         if (rc) return rc;
-        rc = slot_snapshot(e, s, false);
+        for (int i = 0; i < count && !rc; ++i) {
+            st[i].total = st[i].step + (long long)c;
+            st[i].maxerr_bits = 0;
+            st[i].op = OP_PRODUCT;
+            st[i].partner = s + i;
+            rc = slot_write(e, s + i, st[i]);
+        }
         if (rc) return rc;
-        st.total = st.step + (long long)c;
-        st.maxerr_bits = 0;
-        st.op = OP_PRODUCT;
-        st.partner = s;
-        rc = slot_write(e, s, st);
-        if (rc) return rc;
-        if (e->persist && persist_prepare(e->pool)) {
-            rc = pool_run_persist(e->pool, (long long)c, s, 1);
+        // the cooperative kernel is only used for one residue: its first run on
+        // two residues did not finish within the time limit and stays disabled
+        if (e->persist && count == 1 && persist_prepare(e->pool)) {
+            rc = pool_run_persist(e->pool, (long long)c, s, count);
             if (rc == PG_ETIMEOUT) {
-                // a barrier wait ran out: restore the chunk and stay on the per-pass kernels
+                // a barrier wait ran out: stay on the per-pass kernels from now on
                 e->persist = false;
+                if (count != 1) return PG_EROUNDOFF;
                 rc = slot_snapshot(e, s, true);
                 if (rc) return rc;
                 PG_CK(cudaStreamSynchronize(e->pool->stream));
                 continue;
             }
-            if (!rc) {
-                // the persistent kernel does not touch `active`; keep the state coherent
-                SlotState tmp;
-                rc = slot_state(e, s, &tmp);
-            }
         } else {
-            rc = pool_run(e->pool, (long long)c, !(e->flags & PG_FLAG_NO_GRAPH), s, 1);
+            rc = pool_run(e->pool, (long long)c, !(e->flags & PG_FLAG_NO_GRAPH), s, count, count == 1);
         }
         if (rc) return rc;
-        SlotState after;
-        rc = slot_state(e, s, &after);
+        bool bad = false;
+        double err = 0.0;
+        for (int i = 0; i < count && !rc; ++i) {
+            SlotState after;
+            rc = slot_state(e, s + i, &after);
+            const double ei = bits_to_double(after.maxerr_bits);
+            err = std::max(err, ei);
+            bad = bad || ei > 0.4 || after.flags != 0 || after.step != st[i].total;
+        }
         if (rc) return rc;
-        const double err = bits_to_double(after.maxerr_bits);
-        if (err > 0.4 || after.flags != 0 || after.step != st.total) {
-            rc = slot_snapshot(e, s, true);
-            if (rc) return rc;
-            PG_CK(cudaStreamSynchronize(e->pool->stream));
+        if (bad) {
+            if (count == 1) {
+                rc = slot_snapshot(e, s, true);
+                if (rc) return rc;
+                PG_CK(cudaStreamSynchronize(e->pool->stream));
+            }
             rc = engine_bump(e);
             if (rc) return rc;
+            if (count != 1) return PG_EROUNDOFF;
             if (++guard > 8) return PG_EROUNDOFF;
             continue;
         }
@@ -809,7 +835,7 @@ static int run_squarings(pg_engine* e, int s, uint64_t steps) {
 // a <- a * b * 2^-n (Montgomery product); a and b are adjacent slots.
 // Returns PG_EROUNDOFF when the product's roundoff or digits went out of range.
 static int run_product(pg_engine* e, int a, int b) {
-    if (a - b != 1 && b - a != 1) return PG_EINVAL;
+    if (a == b) return PG_EINVAL;  // slots strictly between a and b are idle (step == total)
     SlotState sa, sb;
     int rc = slot_state(e, a, &sa);
     if (!rc) rc = slot_state(e, b, &sb);
@@ -824,7 +850,7 @@ static int run_product(pg_engine* e, int a, int b) {
     sb.partner = b;
     rc = slot_write(e, a, sa);
     if (!rc) rc = slot_write(e, b, sb);
-    if (!rc) rc = pool_run(e->pool, 1, false, std::min(a, b), 2);
+    if (!rc) rc = pool_run(e->pool, 1, false, std::min(a, b), std::abs(a - b) + 1);
     if (rc) return rc;
     SlotState ra, rb;
     rc = slot_state(e, a, &ra);
@@ -855,6 +881,7 @@ static int gz_arm(pg_engine* e, int from) {
         if (!rc && dst != from) rc = slot_copy(e, from, dst);
     e->blocks = 0;
     e->armed = true;
+    e->y_live = false;
     return rc;
 }
 
@@ -870,19 +897,15 @@ static uint64_t gz_rollback(pg_engine* e, int* rc) {
     return redo;
 }
 
-// Verify the completed blocks: Y holds D_{t-1}; check X0 * Y^(2^B) == D.
-static int gz_verify_blocks(pg_engine* e, bool* ok) {
-    *ok = true;
-    if (e->blocks == 0) return PG_OK;
-    int rc = run_squarings(e, SY, e->B);
-    if (rc) return rc;
-    rc = run_product(e, SY, SX0);
+// y <- y * X0, then compare with D.
+static int gz_close(pg_engine* e, int y, bool* ok) {
+    int rc = run_product(e, y, SX0);
     if (rc == PG_EROUNDOFF) {
         *ok = false;
         return PG_OK;
     }
     if (rc) return rc;
-    rc = slots_equal(e, SY, SD, ok);
+    rc = slots_equal(e, y, SD, ok);
     if (rc) return rc;
     if (*ok) {
         e->checks++;
@@ -890,6 +913,21 @@ static int gz_verify_blocks(pg_engine* e, bool* ok) {
         rc = gz_arm(e, SXB);  // the end of the last full block is now verified
     }
     return rc;
+}
+
+// Sequential verification of the completed blocks: YP holds D_{t-1};
+// check X0 * YP^(2^B) == D.
+static int gz_verify_blocks(pg_engine* e, bool* ok) {
+    *ok = true;
+    if (e->blocks == 0) return PG_OK;
+    e->y_live = false;
+    int rc = run_squarings(e, SYP, e->B);
+    if (rc == PG_EROUNDOFF) {
+        *ok = false;
+        return PG_OK;
+    }
+    if (rc) return rc;
+    return gz_close(e, SYP, ok);
 }
 
 static int gz_square(pg_engine* e, uint64_t iters) {
@@ -901,35 +939,53 @@ static int gz_square(pg_engine* e, uint64_t iters) {
     uint64_t owed = iters;
     while (owed > 0) {
         if (e->consecutive_fail > 4) return PG_EGERBICZ;
+        int rc = PG_OK;
+        // The last full block before a verification squares Y = D_{t-1} beside X.
+        if (e->in_block == 0 && !e->y_live && owed >= e->B) {
+            const bool last = e->V ? (e->blocks + 1 == e->V) : (owed < 2ull * e->B);
+            if (last) {
+                rc = slot_copy(e, SD, SY);
+                if (rc) return rc;
+                e->y_live = true;
+            }
+        }
         const uint64_t c = std::min<uint64_t>(owed, e->B - e->in_block);
-        int rc = run_squarings(e, SX, c);
+        rc = e->y_live ? run_squarings(e, SX, c, 2) : run_squarings(e, SX, c);
+        if (rc == PG_EROUNDOFF && e->y_live) {
+            owed += c;  // the pair chunk is redone at the larger length from the verified state
+            owed += gz_rollback(e, &rc);
+            if (rc) return rc;
+            continue;
+        }
         if (rc) return rc;
         e->in_block += c;
         e->squarings += c;
         owed -= c;
-        if (e->in_block == e->B) {
-            // block end: Y = D_{t-1}, D = D * X, XB = X
-            rc = slot_copy(e, SD, SY);
-            if (!rc) rc = run_product(e, SD, SX);
-            if (rc == PG_EROUNDOFF) {
-                owed += gz_rollback(e, &rc);
-                if (rc) return rc;
-                continue;
-            }
+        if (e->in_block < e->B) continue;
+        // block end: YP = D_{t-1}, D = D * X, XB = X
+        rc = slot_copy(e, SD, SYP);
+        if (!rc) rc = run_product(e, SD, SX);
+        if (rc == PG_EROUNDOFF) {
+            owed += gz_rollback(e, &rc);
             if (rc) return rc;
-            rc = slot_copy(e, SX, SXB);
+            continue;
+        }
+        if (rc) return rc;
+        rc = slot_copy(e, SX, SXB);
+        if (rc) return rc;
+        e->blocks++;
+        e->in_block = 0;
+        bool ok = true;
+        if (e->y_live) {
+            e->y_live = false;
+            rc = gz_close(e, SY, &ok);  // Y = D_{t-1}^(2^B)
+        } else if (e->V && e->blocks >= e->V) {
+            rc = gz_verify_blocks(e, &ok);
+        }
+        if (rc) return rc;
+        if (!ok) {
+            owed += gz_rollback(e, &rc);
             if (rc) return rc;
-            e->blocks++;
-            e->in_block = 0;
-            if (e->V && e->blocks >= e->V) {
-                bool ok = true;
-                rc = gz_verify_blocks(e, &ok);
-                if (rc) return rc;
-                if (!ok) {
-                    owed += gz_rollback(e, &rc);
-                    if (rc) return rc;
-                }
-            }
         }
     }
     return PG_OK;
@@ -939,6 +995,7 @@ static int gz_square(pg_engine* e, uint64_t iters) {
 // block (recomputed from XB); on a mismatch, roll back and redo.
 static int gz_flush(pg_engine* e) {
     if (!e->gz || !e->armed) return PG_OK;
+    e->y_live = false;
     for (int guard = 0; guard < 16; ++guard) {
         int rc = PG_OK;
         if (e->blocks > 0) {
@@ -953,10 +1010,14 @@ static int gz_flush(pg_engine* e) {
             }
         }
         if (e->in_block > 0) {
-            rc = slot_copy(e, SXB, SY);
-            if (!rc) rc = run_squarings(e, SY, e->in_block);
+            rc = slot_copy(e, SXB, SYP);
+            if (!rc) rc = run_squarings(e, SYP, e->in_block);
             bool ok = false;
-            if (!rc) rc = slots_equal(e, SY, SX, &ok);
+            if (!rc) rc = slots_equal(e, SYP, SX, &ok);
+            if (rc == PG_EROUNDOFF) {
+                ok = false;
+                rc = PG_OK;
+            }
             if (rc) return rc;
             if (ok) {
                 e->checks++;
@@ -1006,11 +1067,7 @@ const char* pg_strerror(int s) {
     }
 }
 
-int pg_version(void) {
-    const char* e = getenv("PROTH_NO_PDL");
-    if (e && *e == '1') g_use_pdl = false;
-    return 100;
-}
+int pg_version(void) { return 100; }
 
 int pg_device_info(char* name, size_t name_len, int* sm_count) {
     cudaDeviceProp prop;
@@ -1066,7 +1123,7 @@ int pg_create(uint64_t k, uint32_t n, uint32_t fft_len_hint, uint32_t flags, pg_
     e->n = n;
     e->flags = flags;
     e->gz = !(flags & PG_FLAG_NO_GERBICZ);
-    e->persist = !(flags & PG_FLAG_NO_PERSIST);
+    e->persist = (flags & PG_FLAG_PERSIST) != 0;  // per-pass kernels with PDL measured faster
     e->nslots = e->gz ? NSLOTS_GZ : 1;
     int rc = engine_alloc(e, lg);
     if (rc) {
@@ -1222,7 +1279,7 @@ int pg_time_squarings(pg_engine* e, uint64_t iters, double* ms, uint32_t* kernel
     if (e->persist && persist_prepare(e->pool))
         rc = pool_run_persist(e->pool, (long long)iters, SX, 1);
     else
-        rc = pool_run(e->pool, (long long)iters, !(e->flags & PG_FLAG_NO_GRAPH), SX, 1);
+        rc = pool_run(e->pool, (long long)iters, !(e->flags & PG_FLAG_NO_GRAPH), SX, 1, true);
     PG_CK(cudaEventRecord(b, e->pool->stream));
     PG_CK(cudaEventSynchronize(b));
     float f = 0.f;
@@ -1252,7 +1309,7 @@ int pg_profile_step(pg_engine* e, double* times, uint32_t cap, uint32_t* count) 
     for (auto& x : ev) PG_CK(cudaEventCreate(&x));
     PG_CK(cudaEventRecord(ev[0], e->pool->stream));
     for (int i = 0; i < parts && rc == PG_OK; ++i) {
-        rc = enqueue_step_part(e->pool, i, SX, 1);
+        rc = enqueue_step_part(e->pool, i, SX, 1, true);
         cudaEventRecord(ev[i + 1], e->pool->stream);
     }
     PG_CK(cudaEventSynchronize(ev[parts]));

@@ -80,12 +80,12 @@ struct WarpSync {
 struct NoWait {
     __device__ __forceinline__ bool operator()() const { return true; }
 };
-// Programmatic dependent launch: let the next kernel in the stream start its
-// own prologue now, then wait until this kernel's predecessor has completed.
-__device__ __forceinline__ void pdl_wait() {
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-}
+// Programmatic dependent launch: wait until the previous kernel in the stream
+// has completed (its writes visible).  pdl_trigger() at the end of a CTA's
+// work lets the next kernel's CTAs start their prologue during this kernel's
+// tail; triggering earlier would let a whole graph of kernels pile up on the SMs.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 // ... then go on only if the slot is active in this step (and, for the
 // inverse passes, computes a product of its own).
 struct PdlActive {
@@ -94,6 +94,13 @@ struct PdlActive {
     __device__ __forceinline__ bool operator()() const {
         pdl_wait();
         return st->active && !(need_product && st->op == OP_FORWARD);
+    }
+};
+// A single residue whose step count the host controls exactly: only wait.
+struct PdlOnly {
+    __device__ __forceinline__ bool operator()() const {
+        pdl_wait();
+        return true;
     }
 };
 // The first pass decides the step's activity from the counters and publishes it.
@@ -331,10 +338,11 @@ __device__ __forceinline__ void tile_first(const Slot& sl, const PlanDev& pl, in
     const long long nruns = pl.M / RUN;
     const double2* __restrict__ tw = pl.tw[0];
     double2 cw[PER], ct[PER];  // constants, loaded before waiting on the previous kernel
+    const bool bound = sl.wf != nullptr;  // slots of a batch pool may not hold a candidate yet
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
         const int e = tid + i * NT;
-        if (e < F0 * G) {
+        if (e < F0 * G && bound) {
             const int q = e / G, t = e % G;
             cw[i] = sl.wf[r0 + t + q * S0];
             ct[i] = tw[q * S0 + r0 + t];
@@ -485,16 +493,32 @@ __device__ __forceinline__ void tile_last(const Slot& sl, const Slot& pb, const 
     const int r0 = cta * G;
     const double2* __restrict__ tw = pl.tw[0];
     double2 ct[PER], cw[PER];
+    const bool bound = sl.wi != nullptr;  // slots of a batch pool may not hold a candidate yet
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
         const int e = tid + i * NT;
-        if (e < F0 * G) {
+        if (e < F0 * G && bound) {
             const int q = e / G, t = e % G;
             ct[i] = tw[q * S0 + r0 + t];
             cw[i] = sl.wi[r0 + t + q * S0];
         }
     }
     if (!pre()) return;
+    // integer operands of the fold, loaded now so their latency overlaps the transform
+    const unsigned long long j0 = (unsigned long long)r0 + (unsigned long long)tid * S0;
+    int4 v0 = make_int4(0, 0, 0, 0), v1 = v0, w0 = v0, w1 = v0;
+    long long ta_ = 0, tb_ = 0, step_ = 0;
+    if (tid < F0) {
+        const int4* dp = reinterpret_cast<const int4*>(sl.digits + j0);
+        const int4* qp = reinterpret_cast<const int4*>(pb.digits + j0);
+        v0 = dp[0];
+        v1 = dp[1];
+        w0 = qp[0];
+        w1 = qp[1];
+        ta_ = st->top;
+        tb_ = pb.st->top;
+        step_ = st->step;
+    }
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
         const int e = tid + i * NT;
@@ -521,15 +545,11 @@ __device__ __forceinline__ void tile_last(const Slot& sl, const Slot& pb, const 
     if ((tid & 31) == 0 && emax > 0) atomicMax(&st->maxerr_bits, emax);
     sync();
     if (tid < F0) {
-        const unsigned long long j0 = (unsigned long long)r0 + (unsigned long long)tid * S0;
         const long long run = (long long)(j0 / RUN);
-        int4* dp = reinterpret_cast<int4*>(sl.digits + j0);
-        const int4* qp = reinterpret_cast<const int4*>(pb.digits + j0);
-        const int4 v0 = dp[0], v1 = dp[1], w0 = qp[0], w1 = qp[1];
         const int dv[RUN] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
         const int dw[RUN] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
-        const i128 ta = (i128)st->top, tb = (i128)pb.st->top;
-        const i128 s = (i128)sched_mul(st, st->step - 1);
+        const i128 ta = (i128)ta_, tb = (i128)tb_;
+        const i128 s = (i128)sched_mul(st, step_ - 1);
         const i128 kk = (i128)sl.k;
         if (run == 0) store_pend(st, s * ta * tb);
         i128 carry = 0;
@@ -542,6 +562,7 @@ __device__ __forceinline__ void tile_last(const Slot& sl, const Slot& pb, const 
             carry += u;
             nd[t] = (int)take_digit(carry, digit_width(j0 + t, sl.n, pl.lgM));
         }
+        int4* dp = reinterpret_cast<int4*>(sl.digits + j0);
         dp[0] = make_int4(nd[0], nd[1], nd[2], nd[3]);
         dp[1] = make_int4(nd[4], nd[5], nd[6], nd[7]);
         store_carry(sl.carries, run, carry);
@@ -551,33 +572,64 @@ __device__ __forceinline__ void tile_last(const Slot& sl, const Slot& pb, const 
 // ---------------------------------------------------------------------------
 // Per-pass kernels: one tile per CTA, blockIdx.y = slot - base.
 
+// `one` (by value): when its digits pointer is set, the launch squares that
+// single residue (blockIdx.y == 0) for a step count the host controls exactly,
+// so the kernels skip the slot-table load and the activity checks.
+
 template <int F0>
-__global__ void __launch_bounds__(2 * F0) k_first(const Slot* __restrict__ slots, int base, const PlanDev pl) {
+__global__ void __launch_bounds__(2 * F0) k_first(const Slot* __restrict__ slots, int base, const PlanDev pl,
+                                                  const Slot one) {
     __shared__ double2 tile[F0 * RUN];
     __shared__ int dsm[F0 * RUN];
-    const Slot sl = slots[base + blockIdx.y];
-    tile_first<F0, 2 * F0>(sl, pl, blockIdx.x, threadIdx.x, tile, dsm, BlockSync(),
-                           PdlFirst{sl.st, blockIdx.x == 0 && threadIdx.x == 0});
+    if (one.digits) {
+        tile_first<F0, 2 * F0>(one, pl, blockIdx.x, threadIdx.x, tile, dsm, BlockSync(), PdlOnly());
+    } else {
+        const Slot sl = slots[base + blockIdx.y];
+        tile_first<F0, 2 * F0>(sl, pl, blockIdx.x, threadIdx.x, tile, dsm, BlockSync(),
+                               PdlFirst{sl.st, blockIdx.x == 0 && threadIdx.x == 0});
+    }
+    pdl_trigger();
 }
 
 template <int F, int G>
-__global__ void __launch_bounds__(F * G / 4) k_mid_fwd(const Slot* __restrict__ slots, int base, const PlanDev pl) {
+__global__ void __launch_bounds__(F * G / 4) k_mid_fwd(const Slot* __restrict__ slots, int base, const PlanDev pl,
+                                                       const Slot one) {
     __shared__ double2 tile[F * G];
-    const Slot sl = slots[base + blockIdx.y];
-    tile_mid_fwd<F, G, F * G / 4>(sl, pl, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlActive{sl.st, false});
+    if (one.digits) {
+        tile_mid_fwd<F, G, F * G / 4>(one, pl, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlOnly());
+    } else {
+        const Slot sl = slots[base + blockIdx.y];
+        tile_mid_fwd<F, G, F * G / 4>(sl, pl, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlActive{sl.st, false});
+    }
+    pdl_trigger();
 }
 
 template <int F, int G>
-__global__ void __launch_bounds__(F * G / 4) k_mid_inv(const Slot* __restrict__ slots, int base, const PlanDev pl) {
+__global__ void __launch_bounds__(F * G / 4) k_mid_inv(const Slot* __restrict__ slots, int base, const PlanDev pl,
+                                                       const Slot one) {
     __shared__ double2 tile[F * G];
-    const Slot sl = slots[base + blockIdx.y];
-    tile_mid_inv<F, G, F * G / 4>(sl, pl, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlActive{sl.st, true});
+    if (one.digits) {
+        tile_mid_inv<F, G, F * G / 4>(one, pl, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlOnly());
+    } else {
+        const Slot sl = slots[base + blockIdx.y];
+        tile_mid_inv<F, G, F * G / 4>(sl, pl, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlActive{sl.st, true});
+    }
+    pdl_trigger();
 }
 
 template <int F, int G, int LASTP>
-__global__ void __launch_bounds__(F * G / 4) k_inner(const Slot* __restrict__ slots, int base, const PlanDev pl) {
+__global__ void __launch_bounds__(F * G / 4) k_inner(const Slot* __restrict__ slots, int base, const PlanDev pl,
+                                                     const Slot one) {
     __shared__ double2 tile[F * G];
     __shared__ double2 tile2[F * G];
+    if (one.digits) {
+        pdl_wait();
+        if (blockIdx.x == 0 && threadIdx.x == 0) one.st->step += 1;
+        tile_inner<F, G, LASTP, F * G / 4>(one, one, true, pl, blockIdx.x, threadIdx.x, tile, tile2, BlockSync(),
+                                            NoWait());
+        pdl_trigger();
+        return;
+    }
     const Slot sl = slots[base + blockIdx.y];
     SlotState* st = sl.st;
     pdl_wait();
@@ -588,18 +640,25 @@ __global__ void __launch_bounds__(F * G / 4) k_inner(const Slot* __restrict__ sl
     const bool square = partner == base + (int)blockIdx.y;
     tile_inner<F, G, LASTP, F * G / 4>(sl, slots[partner], square, pl, blockIdx.x, threadIdx.x, tile, tile2,
                                         BlockSync(), NoWait());
+    pdl_trigger();
 }
 
 template <int F0>
-__global__ void __launch_bounds__(2 * F0) k_last(const Slot* __restrict__ slots, int base, const PlanDev pl) {
+__global__ void __launch_bounds__(2 * F0) k_last(const Slot* __restrict__ slots, int base, const PlanDev pl,
+                                                 const Slot one) {
     __shared__ double2 tile[F0 * RUN];
     __shared__ long long cl[F0 * RUN];
     __shared__ long long ch[F0 * RUN];
-    const Slot sl = slots[base + blockIdx.y];
-    SlotState* st = sl.st;
-    // the partner index is fixed by the host before the step: safe to read early
-    tile_last<F0, 2 * F0>(sl, slots[st->partner], pl, blockIdx.x, threadIdx.x, tile, cl, ch, BlockSync(),
-                          PdlActive{st, true});
+    if (one.digits) {
+        tile_last<F0, 2 * F0>(one, one, pl, blockIdx.x, threadIdx.x, tile, cl, ch, BlockSync(), PdlOnly());
+    } else {
+        const Slot sl = slots[base + blockIdx.y];
+        SlotState* st = sl.st;
+        // the partner index is fixed by the host before the step: safe to read early
+        tile_last<F0, 2 * F0>(sl, slots[st->partner], pl, blockIdx.x, threadIdx.x, tile, cl, ch, BlockSync(),
+                              PdlActive{st, true});
+    }
+    pdl_trigger();
 }
 
 // ---------------------------------------------------------------------------

@@ -66,6 +66,10 @@ def run_ref(args, cwd, stdin=None):
     return out.stdout
 
 
+def _str_args(args):
+    return [str(a) for a in args]
+
+
 def ref_trace(k, n, L, x0, steps, cwd):
     out = run_ref(["trace", k, n, L, steps, "-"], cwd, stdin=format(x0, "x"))
     rows = [ln.split() for ln in out.strip().splitlines() if ln and ln[0].isdigit()]
@@ -155,6 +159,19 @@ def main():
         g["gmp_tests"].append({"k": k, "n": n, "base": a, "verdict": int(y == N - 1) if a else 0,
                                "res64": format(y & M64, "016x"), "gated": bool(gated)})
         print("gmp test", k, n, flush=True)
+    # 7. a checkpoint file written by the reference's own save_checkpoint
+    k, n = 9999, 32768
+    N = k * (1 << n) + 1
+    L = corrected_L(n, k)
+    a = base_of(k, n)
+    x = _gmp.square_chain(_gmp.powmod(a, k, N), 500, N, every=500)[0]
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "ref_checkpoint_k9999_n32768.bin")
+    subprocess.run([REF] + _str_args(["ckpt_save", k, n, L, 499, path]), input=format(x, "x"), text=True,
+                   check=True)
+    g["ref_checkpoint"] = {"file": os.path.basename(path), "k": k, "n": n, "L": L, "a": a, "current_i": 499,
+                           "squarings_from_a_pow_k": 500, "sha256": digest(x),
+                           "res64_after_300_more": format(_gmp.square_chain(x, 300, N, every=300)[0] & M64, "016x")}
+    print("ref checkpoint written", flush=True)
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.json")
     with open(out, "w") as f:
         json.dump(g, f, indent=1)

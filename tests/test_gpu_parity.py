@@ -43,7 +43,7 @@ def test_device_is_gb300(pg):
 def test_steps_match_python(pg, k, n, path):
     N = _N(k, n)
     x = random.Random(n * 31 + k).randrange(N)
-    flags = pg.FLAG_NO_GRAPH | (pg.FLAG_NO_PERSIST if path == "per-pass" else 0)
+    flags = pg.FLAG_NO_GRAPH | (pg.FLAG_PERSIST if path == "persistent" else 0)
     with pg.Engine(k, n, flags=flags) as e:
         e.set_residue(x)
         assert e.get_residue() == x
@@ -74,7 +74,7 @@ def test_persistent_equals_per_pass_at_full_size(pg, n):
     kernels give identical residues (and equal to Python at the smaller n)."""
     k = 878261
     res = []
-    for flags in (0, pg.FLAG_NO_PERSIST):
+    for flags in (pg.FLAG_PERSIST, 0):
         with pg.Engine(k, n, flags=flags | pg.FLAG_NO_GERBICZ) as e:
             e.set_residue(5)
             e.square(300)
@@ -208,6 +208,21 @@ def test_roundoff_without_bump_reports(pg):
         assert ei.value.status == pg.PG_EROUNDOFF
 
 
+@pytest.mark.parametrize("flags", [0, "nograph"])
+def test_gerbicz_concurrent_verification(pg, flags):
+    """The verification chain squares beside the residue in the last block of
+    each interval; the result and the counters must be right on every path."""
+    f = {0: 0, "nograph": pg.FLAG_NO_GRAPH}[flags]
+    k, n = 878261, 1 << 20
+    N = _N(k, n)
+    with pg.Engine(k, n, flags=f) as e:
+        e.set_gerbicz(100, 3)
+        e.set_residue(5)
+        e.square(700)
+        assert e.stats()["gerbicz_checks"] >= 2 and e.stats()["gerbicz_failures"] == 0
+        assert e.get_residue() == pow(5, 1 << 700, N)
+
+
 def test_gerbicz_clean_run(pg):
     k, n = 12345, 65536
     N = _N(k, n)
@@ -276,3 +291,23 @@ def test_reference_api_shim_is_a_drop_in(pg, gmp, golden):
                              capture_output=True, text=True, check=True).stdout.split("\n")
         got = [ln.split()[1] for ln in out if ln.strip()]
         assert got == t["res64"][:steps], (t["k"], t["n"])
+
+
+def test_resume_from_reference_checkpoint(pg, golden, tmp_path):
+    """A checkpoint file written by the reference's own save_checkpoint loads into
+    the engine; resuming gives the GMP residue, and the engine's file keeps the
+    reference layout."""
+    import shutil
+    import struct
+    c = golden["ref_checkpoint"]
+    src = os.path.join(os.path.dirname(GOLDEN), c["file"])
+    path = str(tmp_path / "check.bin")
+    shutil.copy(src, path)
+    with pg.Engine(c["k"], c["n"]) as e:
+        assert e.checkpoint_load(path) == c["current_i"]
+        e.square(300)
+        assert format(e.get_residue() & M64, "016x") == c["res64_after_300_more"]
+        e.checkpoint_save(path, c["current_i"] + 300)
+    raw = open(path, "rb").read()
+    ci, nl = struct.unpack("<QQ", raw[:16])
+    assert ci == c["current_i"] + 300 and nl == c["L"] // 4

@@ -136,3 +136,18 @@ def test_choose_L_capacity(oracle):
             L = oracle.lib().ora_choose_L(n, k)
             assert n + k.bit_length() + 64 <= 16 * L
             assert L & (L - 1) == 0
+
+
+def test_reference_checkpoint_fixture_layout(golden, gmp):
+    """The checkpoint written by the reference's save_checkpoint: header
+    {uint64 current_i, size_t n_limbs} then little-endian limbs."""
+    import struct
+    c = golden["ref_checkpoint"]
+    raw = open(os.path.join(os.path.dirname(GOLDEN), c["file"]), "rb").read()
+    ci, nl = struct.unpack("<QQ", raw[:16])
+    assert ci == c["current_i"] and nl == c["L"] // 4 and len(raw) == 16 + 8 * nl
+    x = int.from_bytes(raw[16:], "little")
+    N = _N(c["k"], c["n"])
+    want = gmp.square_chain(gmp.powmod(c["a"], c["k"], N), c["squarings_from_a_pow_k"], N,
+                            every=c["squarings_from_a_pow_k"])[0]
+    assert x == want
