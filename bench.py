@@ -127,13 +127,13 @@ PLAN_F = {256: (16, 16), 512: (16, 32), 1024: (32, 32), 2048: (32, 64), 4096: (6
           262144: (64, 64, 64)}
 
 
-def profile_traffic(kernel_regex_name):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, or None."""
-    path = os.path.join(ROOT, "profiles", "k_last_n1048576.txt")
+def profile_traffic():
+    """DRAM bytes of one squaring (its 5 kernels) from the committed ncu launch-list summary, or None."""
+    path = os.path.join(ROOT, "profiles", "squaring_n1048576.md")
     try:
         with open(path) as f:
             for ln in f:
-                if ln.startswith("dram_bytes_per_launch:"):
+                if ln.startswith("dram_bytes_per_squaring:"):
                     return float(ln.split(":", 1)[1])
     except OSError:
         pass
@@ -331,7 +331,7 @@ def run_gpu(args, world, rank, local, pgd):
     dp_ops = dp_ops_per_point(PLAN_F[M]) * M
     dp_rate = dp_ops / t_sq / 1e12                 # T instr/s
     dp_peak = fp64_tflops / 2.0                    # DFMA instr/s from the live probe
-    traffic = profile_traffic("k_last")
+    traffic = profile_traffic()
 
     if rank != 0:
         eng.close()
@@ -351,8 +351,9 @@ def run_gpu(args, world, rank, local, pgd):
                    "fft_bumps": stats["fft_bumps"], "max_err": max_err},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved_gbs / hbm_peak if hbm_peak else None, "traffic": traffic,
-                     "note": "measured hbm_gbs peak; per squaring (the 5 kernels of one squaring); "
-                             "the real bound is the FP64 pipe, see roofline_fp64"},
+                     "note": "measured hbm_gbs peak; unit = one squaring (its 5 kernels); traffic = DRAM "
+                             "bytes of those 5 launches under ncu (cold caches; L2-resident in steady "
+                             "state); the real bound is the FP64 pipe, see roofline_fp64"},
         "roofline_fp64": {"bound": "fp64", "achieved": dp_rate, "peak": dp_peak, "unit": "T DP instr/s",
                           "frac": dp_rate / dp_peak, "dp_instr_per_squaring": dp_ops,
                           "peak_source": "live DFMA probe (pg_measure_fp64_peak), of measured",

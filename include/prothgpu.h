@@ -145,6 +145,13 @@ int pg_checkpoint_load(pg_engine* e, const char* path, uint64_t* current_i);
  * (execute_proth_test_fft, proth_logic.cpp:384-580). */
 int pg_proth_test(uint64_t k, uint32_t n, uint32_t flags, pg_result* out);
 
+/* ---- trial-division pre-filter ----
+ * For each candidate k_i*2^{n_i}+1 the smallest odd prime p < bound (bound <=
+ * 2^32) dividing it, or 0.  Per-candidate counterpart of the reference's GPU
+ * sieve strike (prothlogic4.2/gpu_engine.cu:290-320 check_proth_candidates_kernel),
+ * for a queue of independent (k, n) pairs. */
+int pg_prefilter(const uint64_t* ks, const uint32_t* ns, size_t count, uint64_t bound, uint64_t* smallest_factor);
+
 /* ---- batched engine: many candidates per launch, grouped by FFT length ----
  * Replaces the reference's worker pool (dcore.cpp:84-193 dispatch with
  * worker.cpp:27-69 run_task_with_ctx over PROTH_FF_BATCH k lists). */
@@ -160,6 +167,14 @@ int pg_batch_run(pg_batch* b, uint64_t max_steps);
 int pg_batch_run_timed(pg_batch* b, uint64_t max_steps, double* ms);
 /* Move up to `cap` finished results out; *count receives how many. */
 int pg_batch_poll(pg_batch* b, pg_result* out, size_t cap, size_t* count);
+/* Cap the device bytes that admitted candidates may hold (0: no cap); queued
+ * candidates wait until a verdict frees room.  Class pools are sized to fit. */
+int pg_batch_set_budget(pg_batch* b, uint64_t hbm_bytes);
+/* Test hook: add `delta` to digit `index` of the running candidate `tag`
+ * (a simulated memory error; nothing faults).  PG_ESTATE if it is not running. */
+int pg_batch_debug_corrupt(pg_batch* b, uint64_t tag, uint32_t index, int32_t delta);
+/* Device bytes one candidate k*2^n+1 holds while admitted (slot + checkpoint). */
+uint64_t pg_slot_footprint(uint64_t k, uint32_t n);
 /* Queued, running and finished-but-unpolled candidate counts. */
 int pg_batch_pending(const pg_batch* b, size_t* queued, size_t* running, size_t* finished);
 

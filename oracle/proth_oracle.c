@@ -658,6 +658,22 @@ int ora_proth_test(uint64_t k, unsigned n, size_t L, uint64_t* a_out, uint64_t* 
     return r;
 }
 
+/* Trial division: p | k 2^n + 1  <=>  k 2^n = -1 (mod p), by a plain sieve of
+ * the odd numbers below bound (test sizes: bound up to a few times 10^7). */
+uint64_t ora_smallest_factor(uint64_t k, unsigned n, uint64_t bound) {
+    if (bound < 3) return 0;
+    unsigned char* comp = (unsigned char*)calloc(bound, 1);
+    if (!comp) return 0;
+    uint64_t found = 0;
+    for (uint64_t p = 3; p < bound && !found; p += 2) {
+        if (comp[p]) continue;
+        for (uint64_t j = p * p; j < bound; j += 2 * p) comp[j] = 1;
+        if (mulmod64(k % p, powmod64(2, n, p), p) == p - 1) found = p;
+    }
+    free(comp);
+    return found;
+}
+
 /* ---- CPU baseline: one pinned-style worker per thread, like dcore.cpp:84-193 ---- */
 
 typedef struct {

@@ -92,6 +92,10 @@ int ora_proth_test(uint64_t k, unsigned n, size_t L, uint64_t* a_out, uint64_t* 
 /* Run `iters` reference steps from the canonical residue x (L/4 limbs). */
 double ora_run_squarings(ora_ctx* c, uint64_t* x, unsigned n, uint64_t k, uint64_t iters);
 
+/* Smallest odd prime p < bound dividing k*2^n+1, or 0 (trial division, the
+ * question check_proth_candidates_kernel answers per prime, gpu_engine.cu:290-320). */
+uint64_t ora_smallest_factor(uint64_t k, unsigned n, uint64_t bound);
+
 /* CPU-baseline helper: run `count` independent Proth tests on `threads` POSIX
  * threads (one FFT context per thread, like the reference dispatch), each test
  * truncated to `squarings_per_test` squarings (0 = full test). Returns the wall

@@ -14,7 +14,7 @@ import os
 from . import build as _build_mod
 
 __all__ = ["ProthGpuError", "Engine", "Batch", "proth_test", "execute_proth_test_fft",
-           "load", "pick_fft_len", "gate_rejects", "choose_base", "host_roundtrip"]
+           "load", "pick_fft_len", "gate_rejects", "choose_base", "host_roundtrip", "prefilter"]
 
 PG_OK = 0
 PG_EROUNDOFF = 3
@@ -83,6 +83,7 @@ SIGNATURES = {
     "pg_checkpoint_save": (ctypes.c_int, [_vp, ctypes.c_char_p, _u64]),
     "pg_checkpoint_load": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_u64)]),
     "pg_proth_test": (ctypes.c_int, [_u64, _u32, _u32, ctypes.POINTER(PgResult)]),
+    "pg_prefilter": (ctypes.c_int, [ctypes.POINTER(_u64), ctypes.POINTER(_u32), _sz, _u64, ctypes.POINTER(_u64)]),
     "pg_batch_create": (ctypes.c_int, [_u32, _u32, ctypes.POINTER(_vp)]),
     "pg_batch_destroy": (ctypes.c_int, [_vp]),
     "pg_batch_submit": (ctypes.c_int, [_vp, _u64, _u32, _u64]),
@@ -90,6 +91,9 @@ SIGNATURES = {
     "pg_batch_poll": (ctypes.c_int, [_vp, ctypes.POINTER(PgResult), _sz, ctypes.POINTER(_sz)]),
     "pg_batch_run_timed": (ctypes.c_int, [_vp, _u64, ctypes.POINTER(ctypes.c_double)]),
     "pg_batch_pending": (ctypes.c_int, [_vp, ctypes.POINTER(_sz), ctypes.POINTER(_sz), ctypes.POINTER(_sz)]),
+    "pg_batch_set_budget": (ctypes.c_int, [_vp, _u64]),
+    "pg_batch_debug_corrupt": (ctypes.c_int, [_vp, _u64, _u32, _i32]),
+    "pg_slot_footprint": (_u64, [_u64, _u32]),
 }
 
 
@@ -140,6 +144,21 @@ def launch_count():
 
 def set_device(device):
     _check(load().pg_set_device(device), "pg_set_device")
+
+
+def prefilter(cands, bound=1 << 32):
+    """Smallest odd prime factor < bound of each k*2^n+1 (0 if none), on the GPU."""
+    m = len(cands)
+    ks = (_u64 * max(m, 1))(*[k for k, _ in cands])
+    ns = (_u32 * max(m, 1))(*[n for _, n in cands])
+    out = (_u64 * max(m, 1))()
+    _check(load().pg_prefilter(ks, ns, m, bound, out), "pg_prefilter")
+    return [int(out[i]) for i in range(m)]
+
+
+def slot_footprint(k, n):
+    """Device bytes one admitted candidate holds."""
+    return int(load().pg_slot_footprint(k, n))
 
 
 def pick_fft_len(k, n):
@@ -302,6 +321,13 @@ class Batch:
         cnt = _sz()
         _check(load().pg_batch_poll(self._h, arr, cap, ctypes.byref(cnt)), "pg_batch_poll")
         return [arr[i].as_dict() for i in range(cnt.value)]
+
+    def debug_corrupt(self, tag, index, delta):
+        _check(load().pg_batch_debug_corrupt(self._h, tag, index, delta), "pg_batch_debug_corrupt")
+
+    def set_budget(self, hbm_bytes):
+        """Cap the device bytes held by admitted candidates (admission by HBM footprint)."""
+        _check(load().pg_batch_set_budget(self._h, int(hbm_bytes)), "pg_batch_set_budget")
 
     def pending(self):
         q, r, f = _sz(), _sz(), _sz()

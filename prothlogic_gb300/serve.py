@@ -1,0 +1,129 @@
+"""Serving loop for Proth candidates on one GPU.
+
+Candidates arrive over time (seeded Poisson arrivals; n log-uniform in
+[10000, 300000], k odd in [3, 10^5)).  On arrival they are trial-divided on the
+GPU by every prime below 2^32 (pg_prefilter); survivors are submitted to the
+batched engine (pg_batch), which admits them under an HBM budget (the
+per-candidate device footprint of their FFT length), keeps residues and their
+checkpoints (every 10,000 squarings) on the device, and returns verdicts.
+Reported: p50/p99 time-to-verdict (arrival to verdict) and tests/hour, swept
+over arrival rates until throughput stops growing.
+
+    python -m prothlogic_gb300.serve --rates 2,4,8,16 --window 30
+"""
+import argparse
+import json
+import statistics
+import time
+
+from . import Batch, prefilter, slot_footprint, workloads
+
+
+def _pct(xs, q):
+    if not xs:
+        return None
+    xs = sorted(xs)
+    i = min(len(xs) - 1, max(0, int(round(q / 100.0 * (len(xs) - 1)))))
+    return xs[i]
+
+
+def serve(arrivals, budget_bytes=16 << 30, max_slots=1024, prefilter_bound=1 << 32, slice_steps=400,
+          time_limit=None):
+    """Run the loop over `arrivals` [(t_arrive_s, k, n)] (sorted by time).
+
+    Returns per-candidate records and a summary.  Wall-clock times are host
+    times since the start of the run (the loop is synchronous with the GPU at
+    each slice)."""
+    b = Batch(max_slots)
+    b.set_budget(budget_bytes)
+    t0 = time.perf_counter()
+    i = 0
+    meta = {}
+    records = []
+    busy_s = 0.0
+    while True:
+        now = time.perf_counter() - t0
+        due = []
+        while i < len(arrivals) and arrivals[i][0] <= now:
+            due.append(arrivals[i])
+            i += 1
+        if due:
+            t_pf = time.perf_counter()
+            factors = prefilter([(k, n) for _, k, n in due], bound=prefilter_bound)
+            done_t = time.perf_counter() - t0
+            busy_s += time.perf_counter() - t_pf
+            for (ta, k, n), f in zip(due, factors):
+                if f:
+                    records.append({"k": k, "n": n, "t_arrive": ta, "t_verdict": done_t, "verdict": 0,
+                                    "factor": f, "tested": False})
+                else:
+                    tag = len(meta)
+                    meta[tag] = (ta, k, n)
+                    b.submit(k, n, tag)
+        q, r, f = b.pending()
+        if q + r + f > 0:
+            t_run = time.perf_counter()
+            b.run(slice_steps)
+            busy_s += time.perf_counter() - t_run
+            t_now = time.perf_counter() - t0
+            for res in b.poll():
+                ta, k, n = meta[res["tag"]]
+                records.append({"k": k, "n": n, "t_arrive": ta, "t_verdict": t_now, "verdict": res["verdict"],
+                                "res64": res["res64"], "fft_len": res["fft_len"], "status": res["status"],
+                                "bumps": res["fft_bumps"], "tested": True})
+        elif i < len(arrivals):
+            time.sleep(max(0.0, min(0.5, arrivals[i][0] - (time.perf_counter() - t0))))
+        else:
+            break
+        if time_limit is not None and time.perf_counter() - t0 > time_limit:
+            break
+    wall = time.perf_counter() - t0
+    b.close()
+    tested = [r for r in records if r["tested"]]
+    lat = [r["t_verdict"] - r["t_arrive"] for r in tested]
+    lat_all = [r["t_verdict"] - r["t_arrive"] for r in records]
+    span = max((r["t_verdict"] for r in records), default=0.0)
+    summary = {
+        "arrived": i, "completed": len(records), "prefilter_rejected": len(records) - len(tested),
+        "tested": len(tested), "primes": sum(1 for r in tested if r["verdict"] == 1),
+        "p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99), "p50_all_s": _pct(lat_all, 50),
+        "p99_all_s": _pct(lat_all, 99), "wall_s": wall,
+        "tests_per_hour": len(tested) / span * 3600.0 if span > 0 else 0.0,
+        "candidates_per_hour": len(records) / span * 3600.0 if span > 0 else 0.0,
+        "errors": sum(1 for r in tested if r.get("status", 0) != 0),
+    }
+    return records, summary
+
+
+def sweep(rates, window_s=30.0, seed=5, **kw):
+    """Geometric sweep of arrival rates; stops when tests/hour grows < 10 %."""
+    out = []
+    best = 0.0
+    for lam in rates:
+        count = max(1, int(lam * window_s))
+        arrivals = [(t, k, n) for t, k, n in workloads.serving(count, lam, seed=seed) if t <= window_s]
+        _, s = serve(arrivals, **kw)
+        s["rate_per_s"] = lam
+        s["hbm_footprint_example_bytes"] = slot_footprint(3, 100000)
+        out.append(s)
+        print(json.dumps(s), flush=True)
+        if best and s["tests_per_hour"] < 1.1 * best:
+            break
+        best = max(best, s["tests_per_hour"])
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--rates", default="2,4,8,16,32")
+    ap.add_argument("--window", type=float, default=30.0)
+    ap.add_argument("--budget-gb", type=float, default=16.0)
+    ap.add_argument("--slots", type=int, default=1024)
+    args = ap.parse_args()
+    rates = [float(x) for x in args.rates.split(",")]
+    res = sweep(rates, window_s=args.window, budget_bytes=int(args.budget_gb * (1 << 30)), max_slots=args.slots)
+    print(json.dumps({"sweep": res}))
+
+
+if __name__ == "__main__":
+    main()

@@ -44,6 +44,8 @@ def lib():
                                      ctypes.POINTER(ctypes.c_double), ctypes.POINTER(u64), ctypes.c_size_t]
         L.ora_run_squarings.restype = ctypes.c_double
         L.ora_run_squarings.argtypes = [ctypes.c_void_p, ctypes.POINTER(u64), ctypes.c_uint, u64, u64]
+        L.ora_smallest_factor.restype = u64
+        L.ora_smallest_factor.argtypes = [u64, ctypes.c_uint, u64]
         L.ora_bench_tests.restype = ctypes.c_double
         L.ora_bench_tests.argtypes = [ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_uint), ctypes.c_size_t,
                                       ctypes.c_int, u64, ctypes.POINTER(u64)]

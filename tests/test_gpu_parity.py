@@ -209,7 +209,7 @@ def test_roundoff_without_bump_reports(pg):
 
 
 @pytest.mark.parametrize("flags", [0, "nograph"])
-def test_gerbicz_concurrent_verification(pg, flags):
+def test_gerbicz_concurrent_verification(pg, gmp, flags):
     """The verification chain squares beside the residue in the last block of
     each interval; the result and the counters must be right on every path."""
     f = {0: 0, "nograph": pg.FLAG_NO_GRAPH}[flags]
@@ -220,7 +220,7 @@ def test_gerbicz_concurrent_verification(pg, flags):
         e.set_residue(5)
         e.square(700)
         assert e.stats()["gerbicz_checks"] >= 2 and e.stats()["gerbicz_failures"] == 0
-        assert e.get_residue() == pow(5, 1 << 700, N)
+        assert e.get_residue() == gmp.square_chain(5, 700, N, every=700)[0]
 
 
 def test_gerbicz_clean_run(pg):
@@ -311,3 +311,88 @@ def test_resume_from_reference_checkpoint(pg, golden, tmp_path):
     raw = open(path, "rb").read()
     ci, nl = struct.unpack("<QQ", raw[:16])
     assert ci == c["current_i"] + 300 and nl == c["L"] // 4
+
+
+def test_prefilter_matches_trial_division(pg, oracle):
+    """GPU sieve + Montgomery trial division equals plain trial division."""
+    rng = random.Random(9)
+    cands = [(2 * rng.randrange(1, 50000) + 1, rng.randrange(2048, 300000)) for _ in range(60)]
+    cands += [(3, 2048), (9999, 32768), (843, 120002), (5, 4096)]
+    bound = 1 << 22
+    got = pg.prefilter(cands, bound=bound)
+    for (k, n), f in zip(cands, got):
+        assert f == oracle.lib().ora_smallest_factor(k, n, bound), (k, n)
+        if f:
+            assert (k * pow(2, n, f) + 1) % f == 0
+    assert got[-2] == 0  # 843*2^120002+1 is prime
+
+
+def test_prefilter_full_bound(pg):
+    """Primes up to 2^32: the gate primes are found, and a known prime passes."""
+    cands = [(843, 120002), (3, 2048), (1275, 4399)]
+    got = pg.prefilter(cands, bound=1 << 32)
+    assert got[0] == 0 and got[1] == 19
+    for (k, n), f in zip(cands, got):
+        if f:
+            assert (k * pow(2, n, f) + 1) % f == 0
+
+
+def test_batch_hbm_budget_admission(pg):
+    """Admission by device footprint: with room for two candidates at a time,
+    six still all finish, exactly."""
+    cands = [(2 * i + 3, 4096 + 37 * i) for i in range(6)]
+    fp = pg.slot_footprint(*cands[0])
+    b = pg.Batch(8)
+    b.set_budget(int(2.5 * fp))
+    for i, (k, n) in enumerate(cands):
+        b.submit(k, n, i)
+    b.run(50)
+    q, r, f = b.pending()
+    assert r <= 2
+    b.run(0)
+    res = {x["tag"]: x for x in b.poll()}
+    assert len(res) == 6
+    for i, (k, n) in enumerate(cands):
+        N = _N(k, n)
+        a = res[i]["base"]
+        if a:
+            y = pow(a, (N - 1) // 2, N)
+            assert res[i]["res64"] == y & M64 and res[i]["verdict"] == (y == N - 1)
+    b.close()
+
+
+def test_batch_resumes_from_device_checkpoint(pg, oracle):
+    """A candidate whose digits are corrupted after its 10,000-squaring device
+    checkpoint fails its range check and resumes from that checkpoint, one FFT
+    length up; its verdict and RES64 stay exact."""
+    cands = [(1275, 15013), (99, 15500), (3993, 15700)]
+    b = pg.Batch(4)
+    for i, (k, n) in enumerate(cands):
+        b.submit(k, n, i)
+    b.run(12000)
+    b.debug_corrupt(1, 100, 1 << 30)  # pushes a digit out of its range: the next squaring flags it
+    b.run(0)
+    res = {x["tag"]: x for x in b.poll()}
+    assert len(res) == 3
+    assert res[1]["fft_bumps"] >= 1
+    for i, (k, n) in enumerate(cands):
+        o = oracle.proth_test(k, n)
+        assert (res[i]["verdict"], res[i]["res64"], res[i]["base"]) == (o["verdict"], o["res64"], o["base"])
+    b.close()
+
+
+def test_serving_loop_small(pg):
+    from prothlogic_gb300 import serve
+    arrivals = [(0.05 * i, 2 * (37 * i % 4000) + 3, 6000 + 211 * i) for i in range(16)]
+    recs, s = serve.serve(arrivals, budget_bytes=1 << 30, max_slots=64, prefilter_bound=1 << 24)
+    assert s["completed"] == 16 and s["errors"] == 0
+    assert s["p50_s"] is not None and s["p99_s"] >= s["p50_s"]
+    for r in recs:
+        N = _N(r["k"], r["n"])
+        if r["tested"]:
+            a = pg.choose_base(r["k"], r["n"])
+            if a:
+                y = pow(a, (N - 1) // 2, N)
+                assert r["res64"] == y & M64
+        else:
+            assert N % r["factor"] == 0

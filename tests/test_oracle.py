@@ -151,3 +151,14 @@ def test_reference_checkpoint_fixture_layout(golden, gmp):
     want = gmp.square_chain(gmp.powmod(c["a"], c["k"], N), c["squarings_from_a_pow_k"], N,
                             every=c["squarings_from_a_pow_k"])[0]
     assert x == want
+
+
+def test_oracle_smallest_factor(oracle):
+    rng = random.Random(4)
+    for _ in range(30):
+        k = 2 * rng.randrange(1, 5000) + 1
+        n = rng.randrange(10, 3000)
+        N = _N(k, n)
+        want = next((p for p in range(3, 20000, 2) if all(p % q for q in range(3, int(p ** 0.5) + 1, 2))
+                     and N % p == 0), 0)
+        assert oracle.lib().ora_smallest_factor(k, n, 20000) == want
