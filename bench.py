@@ -372,13 +372,28 @@ def run_gpu(args, world, rank, local, pgd):
     return 0
 
 
+def ncu_target():
+    """Small profiling target: one n = 1,048,576 residue, 200 squarings, no Gerbicz."""
+    import prothlogic_gb300 as pg
+    k, n = workloads.large()
+    e = pg.Engine(k, n, flags=pg.FLAG_NO_GERBICZ)
+    e.set_residue(5)
+    e.square(200)
+    print("res64 %016x" % (e.get_residue() & ((1 << 64) - 1)))
+    e.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ncu-target", action="store_true", help="run only the small profiling target")
     args = ap.parse_args()
+    if args.ncu_target:
+        return ncu_target()
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local, pgd = dist_setup()
