@@ -365,7 +365,8 @@ def test_batch_resumes_from_device_checkpoint(pg, oracle):
     """A candidate whose digits are corrupted after its 10,000-squaring device
     checkpoint fails its range check and resumes from that checkpoint, one FFT
     length up; its verdict and RES64 stay exact."""
-    cands = [(1275, 15013), (99, 15500), (3993, 15700)]
+    cands = [(1275, 15013), (99, 15501), (105, 15500)]
+    assert not any(pg.gate_rejects(k, n) for k, n in cands)  # all three must run
     b = pg.Batch(4)
     for i, (k, n) in enumerate(cands):
         b.submit(k, n, i)
