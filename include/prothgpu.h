@@ -33,6 +33,7 @@ extern "C" {
 #define PG_ENODEV 8     /* no usable sm_103 device */
 #define PG_ESTATE 9     /* handle not ready for this call */
 #define PG_EOVERFLOW 10 /* a digit or carry left its representable range */
+#define PG_ETOOBIG 11   /* request larger than a fixed-size device buffer holds */
 
 /* pg_create flags */
 #define PG_FLAG_NO_GERBICZ 0x1u   /* skip the Gerbicz check in pg_square */
@@ -151,6 +152,24 @@ int pg_proth_test(uint64_t k, uint32_t n, uint32_t flags, pg_result* out);
  * sieve strike (prothlogic4.2/gpu_engine.cu:290-320 check_proth_candidates_kernel),
  * for a queue of independent (k, n) pairs. */
 int pg_prefilter(const uint64_t* ks, const uint32_t* ns, size_t count, uint64_t bound, uint64_t* smallest_factor);
+
+/* Same answer as pg_prefilter, for callers that cannot allocate device memory
+ * (a host runtime that owns the device budget through its own pool, or a
+ * serving loop in which cudaMalloc/cudaFree would synchronise the device).  No
+ * counterpart in the reference.  Allocates nothing: d_ks, d_ns and
+ * d_smallest_factor are DEVICE pointers owned by the caller, the work is queued
+ * on `stream` (a cudaStream_t; NULL = the legacy default stream) and the call
+ * returns without waiting for it.  Its scratch is one file-scope device array
+ * of PG_PREFILTER_NOALLOC_SCRATCH_BYTES, held by every GPU on which the library
+ * is loaded until the process exits; count > PG_PREFILTER_NOALLOC_MAX_COUNT is
+ * rejected with PG_ETOOBIG.  The first call on a device (the current device)
+ * sets the scratch up, synchronously; make that first call before any stream
+ * capture.  All calls share the one array: calls whose work overlaps on the GPU
+ * race and give wrong answers, so order them (one stream, or events). */
+#define PG_PREFILTER_NOALLOC_MAX_COUNT 65536
+#define PG_PREFILTER_NOALLOC_SCRATCH_BYTES 2654464
+int pg_prefilter_noalloc(const uint64_t* d_ks, const uint32_t* d_ns, size_t count, uint64_t bound,
+                         uint64_t* d_smallest_factor, void* stream);
 
 /* ---- batched engine: many candidates per launch, grouped by FFT length ----
  * Replaces the reference's worker pool (dcore.cpp:84-193 dispatch with

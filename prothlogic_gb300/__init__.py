@@ -84,6 +84,7 @@ SIGNATURES = {
     "pg_checkpoint_load": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_u64)]),
     "pg_proth_test": (ctypes.c_int, [_u64, _u32, _u32, ctypes.POINTER(PgResult)]),
     "pg_prefilter": (ctypes.c_int, [ctypes.POINTER(_u64), ctypes.POINTER(_u32), _sz, _u64, ctypes.POINTER(_u64)]),
+    "pg_prefilter_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _sz, _u64, ctypes.c_void_p, ctypes.c_void_p]),
     "pg_batch_create": (ctypes.c_int, [_u32, _u32, ctypes.POINTER(_vp)]),
     "pg_batch_destroy": (ctypes.c_int, [_vp]),
     "pg_batch_submit": (ctypes.c_int, [_vp, _u64, _u32, _u64]),

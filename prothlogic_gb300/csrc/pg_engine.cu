@@ -1063,6 +1063,7 @@ const char* pg_strerror(int s) {
         case PG_ENODEV: return "no sm_103 device";
         case PG_ESTATE: return "handle not ready";
         case PG_EOVERFLOW: return "digit overflow";
+        case PG_ETOOBIG: return "request exceeds the fixed scratch (pg_prefilter_noalloc: at most 65536 candidates)";
         default: return "unknown status";
     }
 }

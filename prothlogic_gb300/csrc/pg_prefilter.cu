@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <vector>
 
@@ -249,4 +250,163 @@ extern "C" int pg_prefilter(const uint64_t* ks, const uint32_t* ns, size_t count
     cudaFree(d_factor);
     if (st) cudaStreamDestroy(st);
     return rc;
+}
+
+// ---- fixed-scratch variant: pg_prefilter_noalloc ----
+//
+// Some callers cannot allocate device memory at all: a host runtime that owns
+// the whole device budget through its own pool and forbids any other
+// allocation in the process, or a latency-bound serving loop in which
+// cudaMalloc/cudaFree would synchronise the device and stall the work queued on
+// other streams.  They hand in device buffers for the candidates and for the
+// result; everything else the pre-filter needs (the base primes, one segment's
+// prime list, two live-candidate lists and their counters) lives in one
+// file-scope device array of fixed size.  Every GPU on which this library is
+// loaded holds that array until the process exits.
+//
+// The kernels are the same sieve as pg_prefilter; the test kernel computes
+// 2^{n_i} mod p per candidate (the live list is not sorted by n, since sorting
+// would need the candidates on the host), and the live list is compacted on the
+// device, so one call is a fixed sequence of launches on the caller's stream
+// with no host synchronisation.
+namespace pgpf {
+
+constexpr unsigned long long kNaSegNumbers = 1ull << 22;        // numbers per sieve launch
+constexpr unsigned kNaPrimeCap = (unsigned)(kNaSegNumbers / 8);  // 2^19 > pi(2^22) = 295,947
+constexpr unsigned kNaBaseCap = 8192;                            // 6,541 odd primes < 2^16
+constexpr unsigned kNaMaxCount = PG_PREFILTER_NOALLOC_MAX_COUNT;
+// Word offsets: counters (segment primes, live count of list 0, of list 1),
+// base primes, segment primes, live list 0, live list 1.
+constexpr size_t kNaOffBase = 64;
+constexpr size_t kNaOffPrimes = kNaOffBase + kNaBaseCap;
+constexpr size_t kNaOffLive0 = kNaOffPrimes + kNaPrimeCap;
+constexpr size_t kNaOffLive1 = kNaOffLive0 + kNaMaxCount;
+constexpr size_t kNaWords = kNaOffLive1 + kNaMaxCount;
+
+__global__ void k_na_seed(uint32_t* __restrict__ ctrl, uint32_t* __restrict__ live0, unsigned count,
+                          unsigned long long* __restrict__ factor) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) {
+        live0[i] = i;
+        factor[i] = ~0ull;
+    }
+    if (i == 0) {
+        ctrl[0] = 0u;
+        ctrl[1] = count;
+        ctrl[2] = 0u;
+    }
+}
+
+// One thread per prime of the segment, every live candidate.
+__global__ void k_na_test(const uint32_t* __restrict__ primes, const uint32_t* __restrict__ nprimes,
+                          const unsigned long long* __restrict__ ks, const uint32_t* __restrict__ ns,
+                          const uint32_t* __restrict__ live, const uint32_t* __restrict__ nlive,
+                          unsigned long long* __restrict__ factor) {
+    const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned np = min(*nprimes, kNaPrimeCap);
+    if (idx >= np) return;
+    const uint32_t p = primes[idx];
+    if (p < 3) return;
+    const Mont M = make_mont(p);
+    const uint32_t minus1 = p - 1;
+    const unsigned nl = *nlive;
+    for (unsigned j = 0; j < nl; ++j) {
+        const uint32_t i = live[j];
+        const uint32_t km = (uint32_t)(ks[i] % p);
+        if (mmul(km, mpow2(ns[i], M), M) == minus1) atomicMin(&factor[i], (unsigned long long)p);
+    }
+}
+
+// Candidates still without a factor move to the other live list.
+__global__ void k_na_compact(const uint32_t* __restrict__ live, const uint32_t* __restrict__ nlive,
+                             const unsigned long long* __restrict__ factor, uint32_t* __restrict__ next,
+                             uint32_t* __restrict__ nnext) {
+    const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= *nlive) return;
+    const uint32_t i = live[j];
+    if (factor[i] == ~0ull) next[atomicAdd(nnext, 1u)] = i;
+}
+
+__global__ void k_na_finish(unsigned long long* __restrict__ factor, unsigned count) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count && factor[i] == ~0ull) factor[i] = 0ull;
+}
+
+}  // namespace pgpf
+
+// The scratch.  In host code this name only stands for the device symbol; its
+// device address comes from cudaGetSymbolAddress, once per device.
+static __device__ __align__(256) uint32_t g_prefilter_scratch[pgpf::kNaWords];
+static_assert(sizeof(g_prefilter_scratch) == PG_PREFILTER_NOALLOC_SCRATCH_BYTES, "scratch size in the header");
+
+namespace {
+
+constexpr int kNaMaxDevices = 64;
+std::mutex g_na_mu;
+uint32_t* g_na_dev[kNaMaxDevices];        // scratch address per device, null until set up
+uint32_t g_na_base[pgpf::kNaBaseCap];    // odd primes < 2^16, ascending
+unsigned g_na_nbase = 0;
+unsigned char g_na_comp[1u << 16];
+
+// First call on a device: find the scratch's device address and write the base
+// primes into it (they never change afterwards).  Runs with that device current.
+int na_setup(uint32_t** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return PG_ECUDA;
+    if (dev < 0 || dev >= kNaMaxDevices) return PG_ENODEV;
+    std::lock_guard<std::mutex> lock(g_na_mu);
+    if (!g_na_nbase) {
+        for (unsigned i = 3; i < (1u << 16); i += 2) {
+            if (g_na_comp[i]) continue;
+            g_na_base[g_na_nbase++] = i;
+            for (unsigned j = i * i; j < (1u << 16); j += 2 * i) g_na_comp[j] = 1;
+        }
+    }
+    if (!g_na_dev[dev]) {
+        void* ptr = nullptr;
+        if (cudaGetSymbolAddress(&ptr, g_prefilter_scratch) != cudaSuccess || !ptr) return PG_ECUDA;
+        uint32_t* s = static_cast<uint32_t*>(ptr);
+        if (cudaMemcpy(s + pgpf::kNaOffBase, g_na_base, g_na_nbase * sizeof(uint32_t), cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+            return PG_ECUDA;
+        g_na_dev[dev] = s;
+    }
+    *out = g_na_dev[dev];
+    return PG_OK;
+}
+
+}  // namespace
+
+extern "C" int pg_prefilter_noalloc(const uint64_t* d_ks, const uint32_t* d_ns, size_t count, uint64_t bound,
+                                    uint64_t* d_smallest_factor, void* stream) {
+    if (count > PG_PREFILTER_NOALLOC_MAX_COUNT) return PG_ETOOBIG;
+    if ((!d_ks || !d_ns || !d_smallest_factor) && count) return PG_EINVAL;
+    if (bound > (1ull << 32) || bound < 3) return PG_EINVAL;
+    if (!count) return PG_OK;
+    uint32_t* s = nullptr;
+    const int rc = na_setup(&s);
+    if (rc != PG_OK) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    uint32_t* ctrl = s;
+    uint32_t* live[2] = {s + kNaOffLive0, s + kNaOffLive1};
+    uint32_t* primes = s + kNaOffPrimes;
+    const unsigned long long* ks = reinterpret_cast<const unsigned long long*>(d_ks);
+    unsigned long long* fac = reinterpret_cast<unsigned long long*>(d_smallest_factor);
+    const unsigned cnt = (unsigned)count;
+    const unsigned cblocks = (cnt + 255) / 256;
+    k_na_seed<<<cblocks, 256, 0, st>>>(ctrl, live[0], cnt, fac);
+    int cur = 0;
+    for (unsigned long long lo = 0; lo < bound; lo += kNaSegNumbers) {
+        if (cudaMemsetAsync(ctrl, 0, sizeof(uint32_t), st) != cudaSuccess) return PG_ECUDA;
+        const unsigned long long limit = std::min<unsigned long long>(bound, lo + kNaSegNumbers);
+        const int ctas = (int)((limit - lo + 2ull * kSubBits - 1) / (2ull * kSubBits));
+        k_sieve<<<ctas, kSieveThreads, 0, st>>>(lo, s + kNaOffBase, (int)g_na_nbase, limit, primes, ctrl,
+                                                kNaPrimeCap);
+        k_na_test<<<kNaPrimeCap / 256, 256, 0, st>>>(primes, ctrl, ks, d_ns, live[cur], ctrl + 1 + cur, fac);
+        if (cudaMemsetAsync(ctrl + 1 + (cur ^ 1), 0, sizeof(uint32_t), st) != cudaSuccess) return PG_ECUDA;
+        k_na_compact<<<cblocks, 256, 0, st>>>(live[cur], ctrl + 1 + cur, fac, live[cur ^ 1], ctrl + 1 + (cur ^ 1));
+        cur ^= 1;
+    }
+    k_na_finish<<<cblocks, 256, 0, st>>>(fac, cnt);
+    return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ECUDA;
 }
