@@ -122,11 +122,6 @@ def dp_ops_per_point(plan_F):
     return first + inner + last
 
 
-PLAN_F = {256: (16, 16), 512: (16, 32), 1024: (32, 32), 2048: (32, 64), 4096: (64, 64), 8192: (64, 128),
-          16384: (128, 128), 32768: (32, 32, 32), 65536: (16, 64, 64), 131072: (32, 64, 64),
-          262144: (64, 64, 64)}
-
-
 def profile_traffic():
     """DRAM bytes of one squaring (its 5 kernels) from the committed ncu launch-list summary, or None."""
     path = os.path.join(ROOT, "profiles", "squaring_n1048576.md")
@@ -223,11 +218,26 @@ def run_reference(args, world, rank, pgd):
     return 0
 
 
+def _chosen(rows):
+    """'f0xf1[xf2] g_mid/g_inner (of N shapes)' for the shape the autotuner picked."""
+    r = [x for x in rows if x["chosen"]][0]
+    radices = "x".join(str(r[f]) for f in ("f0", "f1", "f2")[: r["passes"]])
+    return f"{radices} g{r['g_mid']}/{r['g_inner']} (fastest of {len(rows)} bit-identical shapes)"
+
+
+def _chosen_radices(rows):
+    r = [x for x in rows if x["chosen"]][0]
+    return tuple(r[f] for f in ("f0", "f1", "f2")[: r["passes"]])
+
+
 def batched_sample(pg, steps=300, warm=60):
     """Batched vs one-at-a-time tests/hour at n = 65536 (4096 candidates, k odd in
     [3, 10^6), seed 3), from a bounded sample of squaring steps on the device."""
     cands = workloads.uniform(count=4096)
     n = cands[0][1]
+    lg = pg.pick_fft_len(cands[0][0], n).bit_length() - 1
+    tuned_many = _chosen(pg.autotune(lg, slots=1024, iters=50))
+    tuned_one = _chosen(pg.autotune(lg, slots=1, iters=200))
     b = pg.Batch(4096)
     admitted = 0
     for i, (k, nn) in enumerate(cands):
@@ -254,6 +264,7 @@ def batched_sample(pg, steps=300, warm=60):
             "batched_tests_per_hour": tph_batch, "one_at_a_time_tests_per_hour": tph_single,
             "batched_over_one_at_a_time": tph_batch / tph_single,
             "one_at_a_time_us_per_squaring": us1,
+            "shape_batched": tuned_many, "shape_one_at_a_time": tuned_one,
             "sample": f"{steps} batch squaring steps after {warm} warm-up; one-at-a-time 2000 squarings; "
                       "tests/hour extrapolated to n-1+19 squarings per test; no Gerbicz in either"}
 
@@ -266,6 +277,8 @@ def run_gpu(args, world, rank, local, pgd):
     K, W = args.steps, args.warmup
     peaks = measured_peaks()
     fp64_tflops = pg.measure_fp64_peak()
+    lg = pg.pick_fft_len(k, n).bit_length() - 1
+    tune_rows = pg.autotune(lg, slots=1, iters=200)   # launch shape for one residue at this length
 
     eng = pg.Engine(k, n)
     M = eng.fft_len
@@ -328,7 +341,7 @@ def run_gpu(args, world, rank, local, pgd):
     bytes_alg = 32 * E
     hbm_peak = peaks.get("hbm_gbs")
     achieved_gbs = bytes_alg / t_sq / 1e9
-    dp_ops = dp_ops_per_point(PLAN_F[M]) * M
+    dp_ops = dp_ops_per_point(_chosen_radices(tune_rows)) * M
     dp_rate = dp_ops / t_sq / 1e12                 # T instr/s
     dp_peak = fp64_tflops / 2.0                    # DFMA instr/s from the live probe
     traffic = profile_traffic()
@@ -348,7 +361,7 @@ def run_gpu(args, world, rank, local, pgd):
                    "gerbicz": f"block {SQ_PER_STEP}, {K} blocks verified in the last step",
                    "l2": "flushed between steps (512 MiB write)", "parity_res64": parity,
                    "gerbicz_checks": stats["gerbicz_checks"], "gerbicz_failures": stats["gerbicz_failures"],
-                   "fft_bumps": stats["fft_bumps"], "max_err": max_err},
+                   "fft_bumps": stats["fft_bumps"], "max_err": max_err, "shape": _chosen(tune_rows)},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved_gbs / hbm_peak if hbm_peak else None, "traffic": traffic,
                      "note": "measured hbm_gbs peak; unit = one squaring (its 5 kernels); traffic = DRAM "

@@ -194,6 +194,30 @@ int pg_batch_set_budget(pg_batch* b, uint64_t hbm_bytes);
 int pg_batch_debug_corrupt(pg_batch* b, uint64_t tag, uint32_t index, int32_t delta);
 /* Device bytes one candidate k*2^n+1 holds while admitted (slot + checkpoint). */
 uint64_t pg_slot_footprint(uint64_t k, uint32_t n);
+
+/* ---- launch-shape autotuner (replaces the reference's auto_tune_fft_len,
+ * prothlogic4.2/dcore.cpp:20-81, which tunes only the FFT length) ----
+ * A shape is the pass radices of one squaring at 2^lg points (passes x f0 x
+ * f1 [x f2]) and the transform columns per CTA of the middle and inner kernels
+ * (g_mid, g_inner), i.e. the CTAs per residue.  pg_autotune times every compiled
+ * shape on `slots` residues for >= iters squarings, checks that all shapes give
+ * bit-identical residues, and makes the fastest the shape of later engines
+ * (slots == 1, mode PG_TUNE_ONE) or batch classes (slots > 1, PG_TUNE_MANY) at
+ * that length.  `out` receives up to `cap` rows, `count` the number of shapes. */
+#define PG_TUNE_ONE 0u
+#define PG_TUNE_MANY 1u
+typedef struct pg_tune_result {
+    uint32_t lg, slots, passes, f0, f1, f2, g_mid, g_inner;
+    double us_per_step; /* one squaring of every slot */
+    int32_t valid;      /* residues equal to the other shapes', no roundoff or range flag */
+    int32_t chosen;
+} pg_tune_result;
+int pg_autotune(uint32_t lg, uint32_t slots, uint32_t iters, pg_tune_result* out, size_t cap, size_t* count);
+/* The shape in use for (lg, mode); PG_ESTATE when none was tuned or set. */
+int pg_tune_get(uint32_t lg, uint32_t mode, pg_tune_result* out);
+/* Install a shape (e.g. one saved from an earlier run); PG_EINVAL if not compiled. */
+int pg_tune_set(uint32_t mode, const pg_tune_result* r);
+int pg_tune_clear(void);
 /* Queued, running and finished-but-unpolled candidate counts. */
 int pg_batch_pending(const pg_batch* b, size_t* queued, size_t* running, size_t* finished);
 

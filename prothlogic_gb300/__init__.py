@@ -19,6 +19,8 @@ __all__ = ["ProthGpuError", "Engine", "Batch", "proth_test", "execute_proth_test
 PG_OK = 0
 PG_EROUNDOFF = 3
 PG_EGERBICZ = 4
+PG_ESTATE = 9
+PG_ETOOBIG = 11
 FLAG_NO_GERBICZ = 0x1
 FLAG_NO_BUMP = 0x2
 FLAG_NO_GRAPH = 0x4
@@ -38,6 +40,15 @@ class PgResult(ctypes.Structure):
                 ("res64", _u64), ("tag", _u64), ("fft_len", _u32), ("fft_bumps", _u32),
                 ("gerbicz_checks", _u32), ("gerbicz_failures", _u32), ("max_err", ctypes.c_double),
                 ("seconds", ctypes.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class PgTuneResult(ctypes.Structure):
+    _fields_ = [("lg", _u32), ("slots", _u32), ("passes", _u32), ("f0", _u32), ("f1", _u32), ("f2", _u32),
+                ("g_mid", _u32), ("g_inner", _u32), ("us_per_step", ctypes.c_double), ("valid", _i32),
+                ("chosen", _i32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -95,7 +106,13 @@ SIGNATURES = {
     "pg_batch_set_budget": (ctypes.c_int, [_vp, _u64]),
     "pg_batch_debug_corrupt": (ctypes.c_int, [_vp, _u64, _u32, _i32]),
     "pg_slot_footprint": (_u64, [_u64, _u32]),
+    "pg_autotune": (ctypes.c_int, [_u32, _u32, _u32, ctypes.POINTER(PgTuneResult), _sz, ctypes.POINTER(_sz)]),
+    "pg_tune_get": (ctypes.c_int, [_u32, _u32, ctypes.POINTER(PgTuneResult)]),
+    "pg_tune_set": (ctypes.c_int, [_u32, ctypes.POINTER(PgTuneResult)]),
+    "pg_tune_clear": (ctypes.c_int, []),
 }
+
+TUNE_ONE, TUNE_MANY = 0, 1
 
 
 def load(build_if_missing=True):
@@ -160,6 +177,37 @@ def prefilter(cands, bound=1 << 32):
 def slot_footprint(k, n):
     """Device bytes one admitted candidate holds."""
     return int(load().pg_slot_footprint(k, n))
+
+
+def autotune(lg, slots=1, iters=200):
+    """Time every compiled launch shape at 2^lg points on `slots` residues; the
+    fastest bit-exact one becomes the shape of later engines (slots == 1) or
+    batch classes (slots > 1) at that length.  Returns one dict per shape."""
+    cap = 256
+    out = (PgTuneResult * cap)()
+    cnt = _sz()
+    _check(load().pg_autotune(lg, slots, iters, out, cap, ctypes.byref(cnt)), f"pg_autotune(lg={lg})")
+    return [out[i].as_dict() for i in range(min(cap, cnt.value))]
+
+
+def tune_get(lg, mode=TUNE_ONE):
+    """Shape in use at 2^lg points for `mode`, or None when none was tuned or set."""
+    r = PgTuneResult()
+    rc = load().pg_tune_get(lg, mode, ctypes.byref(r))
+    if rc == PG_ESTATE:
+        return None
+    _check(rc, "pg_tune_get")
+    return r.as_dict()
+
+
+def tune_set(mode, shape):
+    """Install a shape dict (as returned by autotune/tune_get) for `mode`."""
+    r = PgTuneResult(**{f: shape[f] for f, _ in PgTuneResult._fields_ if f in shape})
+    _check(load().pg_tune_set(mode, ctypes.byref(r)), "pg_tune_set")
+
+
+def tune_clear():
+    _check(load().pg_tune_clear(), "pg_tune_clear")
 
 
 def pick_fft_len(k, n):

@@ -51,6 +51,16 @@ struct Plan {
     double2* mem = nullptr;
 };
 
+// A launch shape: the pass radices (which fix the plan and the spectrum order)
+// and the transform columns per CTA of the middle and inner kernels (which fix
+// the CTAs per residue).  Mode 0: one residue per launch; mode 1: many.
+struct Shape {
+    int P = 0;
+    int F[MAX_PASSES] = {0, 0, 0};
+    int gm = 0, gi = 0;
+};
+static std::map<std::pair<int, int>, Shape> g_tuned;  // (lg, mode) -> autotuned shape
+
 static const int kMinLg = 8, kMaxLg = 18;
 static const double kMinBitsPerDigit = 6.0;   // below this the run carries do not settle
 static const double kMaxBitsPerDigit = 24.0;  // balanced digits stay within int32 with room for carries
@@ -99,11 +109,21 @@ static std::vector<int> stage_perm(int F) {
 }
 
 static std::mutex g_cache_mu;
-static std::map<int, Plan*> g_plans;  // keyed by lgM (per process, current device)
+static std::map<std::vector<int>, Plan*> g_plans;  // keyed by (lgM, radices) (per process, current device)
 
-static int get_plan(int lg, Plan** out) {
+// Plan for 2^lg points with the given radices (F == nullptr: the default ones).
+static int get_plan(int lg, Plan** out, const int* F = nullptr, int P = 0) {
+    int Fd[MAX_PASSES] = {0, 0, 0};
+    int Pd = 0;
+    if (F) {
+        Pd = P;
+        for (int i = 0; i < P; ++i) Fd[i] = F[i];
+    } else if (!plan_radices(lg, Fd, Pd)) {
+        return PG_EINVAL;
+    }
+    const std::vector<int> key = {lg, Fd[0], Fd[1], Fd[2]};
     std::lock_guard<std::mutex> lk(g_cache_mu);
-    auto it = g_plans.find(lg);
+    auto it = g_plans.find(key);
     if (it != g_plans.end()) {
         *out = it->second;
         return PG_OK;
@@ -111,10 +131,8 @@ static int get_plan(int lg, Plan** out) {
     Plan* p = new Plan();
     PlanDev& d = p->dev;
     memset(&d, 0, sizeof(d));
-    if (!plan_radices(lg, d.F, d.P)) {
-        delete p;
-        return PG_EINVAL;
-    }
+    d.P = Pd;
+    for (int i = 0; i < Pd; ++i) d.F[i] = Fd[i];
     d.M = 1 << lg;
     d.lgM = lg;
     int Mi = d.M;
@@ -154,7 +172,7 @@ static int get_plan(int lg, Plan** out) {
     p->Ginner_big = (Fl >= 128) ? 4 : 8;
     p->Gmid_small = 2;
     p->Gmid_big = 8;
-    g_plans[lg] = p;
+    g_plans[key] = p;
     *out = p;
     return PG_OK;
 }
@@ -256,6 +274,7 @@ struct Pool {
     cudaStream_t stream = nullptr;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (base, count) -> GSTEPS-step graph
     bool big = false;
+    int gm[2] = {2, 2}, gi[2] = {2, 2};  // middle / inner columns per CTA: [0] one residue per launch, [1] many
     bool capturing = false;
     GridBar* bar = nullptr;      // grid barrier of the persistent kernel
     int persist_grid = 0;        // co-resident CTAs for it (0: not available)
@@ -324,8 +343,8 @@ static int enqueue_step_part(Pool* p, int part, int base, int count, bool solo) 
     memset(&one, 0, sizeof(one));
     if (solo) one = p->hslots[base];
     const dim3 g0(d.S[0] / RUN, count);
-    const int Gm = p->big ? p->plan->Gmid_big : p->plan->Gmid_small;
-    const int Gi = p->big ? p->plan->Ginner_big : p->plan->Ginner_small;
+    const int Gm = p->gm[count == 1 ? 0 : 1];
+    const int Gi = p->gi[count == 1 ? 0 : 1];
     const int Fl = d.F[d.P - 1];
     int nl = 0;
     if (part == 0) {
@@ -387,15 +406,53 @@ static void pool_free(Pool* p) {
     delete p;
 }
 
-static int pool_create(int lg, int S, Pool** out) {
+// Pool of S slots at 2^lg points.  With an explicit shape its radices and
+// columns are used for every launch; otherwise the autotuned shape of `mode`
+// (0: the pool runs one residue per launch, 1: many) when there is one, else
+// the default plan.  The other mode keeps the default columns unless it was
+// tuned with the same radices.
+static int pool_create(int lg, int S, Pool** out, int mode = 0, const Shape* shape = nullptr) {
+    Shape sh;
+    bool have = false;
+    if (shape) {
+        sh = *shape;
+        have = true;
+    } else {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        auto it = g_tuned.find(std::make_pair(lg, mode));
+        if (it != g_tuned.end()) {
+            sh = it->second;
+            have = true;
+        }
+    }
     Plan* plan = nullptr;
-    int rc = get_plan(lg, &plan);
+    int rc = have ? get_plan(lg, &plan, sh.F, sh.P) : get_plan(lg, &plan);
     if (rc) return rc;
     Pool* p = new Pool();
     p->plan = plan;
     p->S = S;
     p->M = 1u << lg;
     p->big = (S > 4);
+    for (int m = 0; m < 2; ++m) {
+        p->gm[m] = p->big ? plan->Gmid_big : plan->Gmid_small;
+        p->gi[m] = p->big ? plan->Ginner_big : plan->Ginner_small;
+    }
+    if (have && shape) {
+        p->gm[0] = p->gm[1] = sh.gm;
+        p->gi[0] = p->gi[1] = sh.gi;
+    } else {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        for (int m = 0; m < 2; ++m) {
+            auto it = g_tuned.find(std::make_pair(lg, m));
+            if (it == g_tuned.end()) continue;
+            const Shape& t = it->second;
+            if (t.P == plan->dev.P && t.F[0] == plan->dev.F[0] && t.F[1] == plan->dev.F[1] &&
+                t.F[2] == plan->dev.F[2]) {
+                p->gm[m] = t.gm;
+                p->gi[m] = t.gi;
+            }
+        }
+    }
     p->hslots.resize(S);
     p->slot_n.assign(S, 0);
     const size_t M = p->M, nruns = M / RUN;
@@ -1403,3 +1460,4 @@ int pg_debug_corrupt(pg_engine* e, uint32_t index, int32_t delta) {
 }  // extern "C"
 
 #include "pg_engine_more.inc"
+#include "pg_tune.inc"

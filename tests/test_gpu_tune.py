@@ -1,0 +1,93 @@
+"""Launch-shape autotuner: every compiled shape must give the same residues as
+GMP, the tuner must pick one, and engines / batches built after tuning must
+stay bit-exact under the tuned shape."""
+import json
+import os
+import random
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden.json")
+M64 = (1 << 64) - 1
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import prothlogic_gb300 as pgm
+    pgm.load()
+    pgm.tune_clear()
+    yield pgm
+    pgm.tune_clear()  # later tests use the default shapes
+
+
+def test_autotune_one_residue_picks_a_valid_shape(pg):
+    rows = pg.autotune(12, slots=1, iters=50)
+    assert len(rows) >= 3
+    assert all(r["valid"] == 1 for r in rows), rows  # all shapes bit-identical
+    chosen = [r for r in rows if r["chosen"]]
+    assert len(chosen) == 1
+    assert chosen[0]["us_per_step"] == min(r["us_per_step"] for r in rows)
+    got = pg.tune_get(12, pg.TUNE_ONE)
+    assert (got["f0"], got["f1"], got["g_inner"]) == (chosen[0]["f0"], chosen[0]["f1"], chosen[0]["g_inner"])
+
+
+@pytest.mark.parametrize("k,n", [(1000003, 400000), (999999, 1500000)])
+def test_every_shape_is_exact_against_gmp(pg, gmp, k, n):
+    """Each compiled shape at the length of (k, n), set by hand, squares a random
+    residue 60 times exactly."""
+    lg = pg.pick_fft_len(k, n).bit_length() - 1
+    rows = pg.autotune(lg, slots=1, iters=50)
+    N = k * (1 << n) + 1
+    x = random.Random(lg).randrange(N)
+    want = gmp.square_chain(x, 60, N, every=60)[0]
+    for r in rows:
+        pg.tune_set(pg.TUNE_ONE, r)
+        with pg.Engine(k, n, flags=pg.FLAG_NO_GERBICZ) as e:
+            e.set_residue(x)
+            e.square(60)
+            assert e.get_residue() == want, r
+    pg.tune_clear()
+
+
+def test_tuned_engine_matches_large_configuration(pg):
+    """n = 2^20 under the shape the tuner picks: RES64 after 1,000 and 2,000
+    squarings equal the GMP values."""
+    with open(GOLDEN) as f:
+        g = json.load(f)["large"]
+    pg.autotune(16, slots=1, iters=100)
+    assert pg.tune_get(16, pg.TUNE_ONE) is not None
+    with pg.Engine(g["k"], g["n"]) as e:
+        e.set_residue(g["a"])
+        for i in range(2):
+            e.square(g["every"])
+            assert format(e.get_residue() & M64, "016x") == g["res64"][i], i
+    pg.tune_clear()
+
+
+def test_tuned_batch_full_tests_exact(pg, gmp):
+    rows = pg.autotune(12, slots=64, iters=50)
+    assert any(r["chosen"] for r in rows) and all(r["valid"] for r in rows)
+    rng = random.Random(12)
+    cands = [(2 * rng.randrange(1, 500000) + 1, 65536) for _ in range(6)]
+    b = pg.Batch(16)
+    for i, (k, n) in enumerate(cands):
+        b.submit(k, n, i)
+    b.run(0)
+    res = {r["tag"]: r for r in b.poll()}
+    assert len(res) == len(cands)
+    for i, (k, n) in enumerate(cands):
+        N = k * (1 << n) + 1
+        a = res[i]["base"]
+        if a:
+            y = gmp.powmod(a, (N - 1) // 2, N)
+            assert res[i]["res64"] == y & M64 and res[i]["verdict"] == (y == N - 1)
+    b.close()
+    pg.tune_clear()
+
+
+def test_tune_set_rejects_shapes_that_are_not_compiled(pg):
+    bad = {"lg": 12, "slots": 1, "passes": 2, "f0": 16, "f1": 256, "f2": 0, "g_mid": 2, "g_inner": 2}
+    with pytest.raises(pg.ProthGpuError):
+        pg.tune_set(pg.TUNE_ONE, bad)
