@@ -20,6 +20,7 @@ Multi-GPU: candidates do not shard, so N > 1 runs N independent replicas
 (one process per GPU) and `value` is the whole-job time per squaring.
 """
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -222,12 +223,84 @@ def _chosen(rows):
     """'f0xf1[xf2] g_mid/g_inner (of N shapes)' for the shape the autotuner picked."""
     r = [x for x in rows if x["chosen"]][0]
     radices = "x".join(str(r[f]) for f in ("f0", "f1", "f2")[: r["passes"]])
-    return f"{radices} g{r['g_mid']}/{r['g_inner']} (fastest of {len(rows)} bit-identical shapes)"
+    return (f"{radices} g{r['g_mid']}/{r['g_inner']} {r['tpb']} thread(s)/butterfly "
+            f"(fastest of {len(rows)} bit-identical shapes)")
 
 
 def _chosen_radices(rows):
     r = [x for x in rows if x["chosen"]][0]
     return tuple(r[f] for f in ("f0", "f1", "f2")[: r["passes"]])
+
+
+def cpu_tests_per_hour(cands, sq_sample, budget_s=None):
+    """Reference-algorithm tests/hour on all host cores (one test per thread, as the
+    reference's dispatcher runs them, prothlogic4.2/dcore.cpp:125-188), from every
+    candidate truncated to `sq_sample` squarings and scaled to its full n - 1."""
+    from tests import _oracle
+    threads = os.cpu_count() or 1
+    count = len(cands)
+    ks = (ctypes.c_uint64 * count)(*[k for k, _ in cands])
+    ns = (ctypes.c_uint * count)(*[n for _, n in cands])
+    wall = _oracle.lib().ora_bench_tests(ks, ns, count, threads, sq_sample, None)
+    # each test also runs the a^k powering (bitlen(k) - 1 squarings) before its chain
+    pow_sq = statistics.mean(max(0, k.bit_length() - 1) for k, _ in cands)
+    full = statistics.mean(n - 1 for _, n in cands) + pow_sq
+    scale = full / (sq_sample + pow_sq)
+    return {"tests_per_hour": count * 3600.0 / (wall * scale), "cores": threads, "kind": "port",
+            "sample": f"{count} tests on {threads} threads, each truncated to {sq_sample} squarings "
+                      f"({wall:.1f} s), scaled by {scale:.0f} to full tests"}
+
+
+def uneven_sample(pg, steps=200, warm=50, cpu_sq=60):
+    """Uneven batch: 2,048 candidates, n log-uniform in [8192, 262144], k odd < 10^5
+    (seed 4), every FFT-length class batched with its autotuned shape.  Per class:
+    device time per squaring step with all its candidates resident, and one
+    candidate alone; tests/hour = candidates / sum over them of (n-1+pow) x the
+    per-candidate cost of their class (classes run one after another)."""
+    cands = [(k, n) for k, n in workloads.uneven(count=2048) if not pg.gate_rejects(k, n)]
+    classes = {}
+    for k, n in cands:
+        classes.setdefault(pg.pick_fft_len(k, n).bit_length() - 1, []).append((k, n))
+    t_batch = t_one = 0.0
+    per_class = {}
+    for lg, members in sorted(classes.items()):
+        tm = _chosen(pg.autotune(lg, slots=min(len(members), 1024), iters=50))
+        b = pg.Batch(len(members))
+        for i, (k, n) in enumerate(members):
+            b.submit(k, n, i)
+        b.run_timed(warm)
+        ms = b.run_timed(steps)
+        _, running, _ = b.pending()
+        b.close()
+        per_cand_sq = ms * 1e-3 / steps / max(1, running)
+        to = _chosen(pg.autotune(lg, slots=1, iters=200))
+        k0, n0 = members[0]
+        e = pg.Engine(k0, n0, flags=pg.FLAG_NO_GERBICZ)
+        e.set_residue(3)
+        e.time_squarings(100)
+        ms1, _ = e.time_squarings(500)
+        e.close()
+        one_sq = ms1 * 1e-3 / 500
+        work = sum(n - 1 + max(0, k.bit_length() - 1) for k, n in members)
+        t_batch += work * per_cand_sq
+        t_one += work * one_sq
+        per_class[f"2^{lg}"] = {"candidates": len(members), "running": running,
+                                "batch_us_per_candidate_squaring": per_cand_sq * 1e6,
+                                "one_at_a_time_us_per_squaring": one_sq * 1e6,
+                                "shape_batched": tm, "shape_one_at_a_time": to}
+    pg.tune_clear()
+    tph_batch = len(cands) * 3600.0 / t_batch
+    tph_one = len(cands) * 3600.0 / t_one
+    cpu = cpu_tests_per_hour(cands, cpu_sq)
+    return {"workload": "uneven: 2048 candidates, n log-uniform in [8192, 262144], k odd in [3,10^5) seed 4",
+            "tested": len(cands), "classes": per_class,
+            "batched_tests_per_hour": tph_batch, "one_at_a_time_tests_per_hour": tph_one,
+            "batched_over_one_at_a_time": tph_batch / tph_one,
+            "cpu_reference_tests_per_hour": cpu["tests_per_hour"],
+            "batched_over_cpu": tph_batch / cpu["tests_per_hour"], "cpu": cpu,
+            "sample": f"per class {steps} batch squaring steps after {warm} warm-up and 500 squarings of one "
+                      "candidate alone; tests/hour extrapolated to each candidate's full chain; "
+                      f"{len(cands)} of 2048 pass the reference's gate (the rest are composite at once)"}
 
 
 def batched_sample(pg, steps=300, warm=60):
@@ -259,12 +332,17 @@ def batched_sample(pg, steps=300, warm=60):
     e.close()
     us1 = ms1 * 1e3 / 2000
     tph_single = 3600.0 / (us1 * 1e-6 * sq_per_test)
+    passing = [(k, nn) for k, nn in cands if not pg.gate_rejects(k, nn)]
+    cpu = cpu_tests_per_hour(passing[: 4 * (os.cpu_count() or 1)], 200)
+    pg.tune_clear()
     return {"workload": "uniform: 4096 candidates, n=65536, k odd in [3,10^6) seed 3",
             "running_slots": admitted, "batch_step_ms": per_step_ms,
             "batched_tests_per_hour": tph_batch, "one_at_a_time_tests_per_hour": tph_single,
             "batched_over_one_at_a_time": tph_batch / tph_single,
             "one_at_a_time_us_per_squaring": us1,
             "shape_batched": tuned_many, "shape_one_at_a_time": tuned_one,
+            "cpu_reference_tests_per_hour": cpu["tests_per_hour"],
+            "batched_over_cpu": tph_batch / cpu["tests_per_hour"], "cpu": cpu,
             "sample": f"{steps} batch squaring steps after {warm} warm-up; one-at-a-time 2000 squarings; "
                       "tests/hour extrapolated to n-1+19 squarings per test; no Gerbicz in either"}
 
@@ -351,6 +429,7 @@ def run_gpu(args, world, rank, local, pgd):
         return 0
     eng.close()
     batched = batched_sample(pg) if os.environ.get("PROTH_BENCH_BATCH", "1") == "1" else None
+    uneven = uneven_sample(pg) if os.environ.get("PROTH_BENCH_UNEVEN", "1") == "1" else None
     cpu_ns, cpu_kind, cpu_used, cpu_L = time_cpu_reference(k, n, a, cpu_sample_seconds())
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -380,8 +459,34 @@ def run_gpu(args, world, rank, local, pgd):
         "clocks": clocks,
         "gpu_launches": launches,
         "batched": batched,
+        "batched_uneven": uneven,
     }
     print(json.dumps(line), flush=True)
+    return 0
+
+
+def uneven_full():
+    """The whole uneven workload (2,048 candidates, every class, autotuned shapes)
+    through one batch to the last verdict; wall-clock tests/hour."""
+    import prothlogic_gb300 as pg
+    cands = workloads.uneven(count=2048)
+    lgs = sorted({pg.pick_fft_len(k, n).bit_length() - 1 for k, n in cands})
+    for lg in lgs:
+        members = sum(1 for k, n in cands if pg.pick_fft_len(k, n).bit_length() - 1 == lg)
+        pg.autotune(lg, slots=min(members, 1024), iters=50)
+    b = pg.Batch(2048)
+    t0 = time.perf_counter()
+    for i, (k, n) in enumerate(cands):
+        b.submit(k, n, i)
+    b.run(0)
+    wall = time.perf_counter() - t0
+    res = b.poll()
+    b.close()
+    tested = sum(1 for r in res if r["base"])
+    print(json.dumps({"workload": "uneven: 2048 candidates, n log-uniform in [8192, 262144], k odd in [3,10^5) seed 4",
+                      "verdicts": len(res), "tested": tested, "primes": sum(1 for r in res if r["verdict"] == 1),
+                      "errors": sum(1 for r in res if r["status"] != 0), "wall_s": wall,
+                      "tests_per_hour": tested * 3600.0 / wall, "classes": [f"2^{lg}" for lg in lgs]}))
     return 0
 
 
@@ -404,9 +509,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ncu-target", action="store_true", help="run only the small profiling target")
+    ap.add_argument("--uneven-full", action="store_true", help="run the whole uneven batch to completion")
     args = ap.parse_args()
     if args.ncu_target:
         return ncu_target()
+    if args.uneven_full:
+        return uneven_full()
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local, pgd = dist_setup()

@@ -198,8 +198,8 @@ uint64_t pg_slot_footprint(uint64_t k, uint32_t n);
 /* ---- launch-shape autotuner (replaces the reference's auto_tune_fft_len,
  * prothlogic4.2/dcore.cpp:20-81, which tunes only the FFT length) ----
  * A shape is the pass radices of one squaring at 2^lg points (passes x f0 x
- * f1 [x f2]) and the transform columns per CTA of the middle and inner kernels
- * (g_mid, g_inner), i.e. the CTAs per residue.  pg_autotune times every compiled
+ * f1 [x f2]), the transform columns per CTA of the middle and inner kernels
+ * (g_mid, g_inner), i.e. the CTAs per residue, and the threads per butterfly.  pg_autotune times every compiled
  * shape on `slots` residues for >= iters squarings, checks that all shapes give
  * bit-identical residues, and makes the fastest the shape of later engines
  * (slots == 1, mode PG_TUNE_ONE) or batch classes (slots > 1, PG_TUNE_MANY) at
@@ -208,6 +208,7 @@ uint64_t pg_slot_footprint(uint64_t k, uint32_t n);
 #define PG_TUNE_MANY 1u
 typedef struct pg_tune_result {
     uint32_t lg, slots, passes, f0, f1, f2, g_mid, g_inner;
+    uint32_t tpb;       /* threads per radix-4 butterfly: 1, or 2 (paired lanes, shorter FP64 chains) */
     double us_per_step; /* one squaring of every slot */
     int32_t valid;      /* residues equal to the other shapes', no roundoff or range flag */
     int32_t chosen;

@@ -47,7 +47,7 @@ class PgResult(ctypes.Structure):
 
 class PgTuneResult(ctypes.Structure):
     _fields_ = [("lg", _u32), ("slots", _u32), ("passes", _u32), ("f0", _u32), ("f1", _u32), ("f2", _u32),
-                ("g_mid", _u32), ("g_inner", _u32), ("us_per_step", ctypes.c_double), ("valid", _i32),
+                ("g_mid", _u32), ("g_inner", _u32), ("tpb", _u32), ("us_per_step", ctypes.c_double), ("valid", _i32),
                 ("chosen", _i32)]
 
     def as_dict(self):
@@ -203,6 +203,8 @@ def tune_get(lg, mode=TUNE_ONE):
 def tune_set(mode, shape):
     """Install a shape dict (as returned by autotune/tune_get) for `mode`."""
     r = PgTuneResult(**{f: shape[f] for f, _ in PgTuneResult._fields_ if f in shape})
+    if "tpb" not in shape:
+        r.tpb = 1
     _check(load().pg_tune_set(mode, ctypes.byref(r)), "pg_tune_set")
 
 

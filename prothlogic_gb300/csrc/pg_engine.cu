@@ -58,6 +58,7 @@ struct Shape {
     int P = 0;
     int F[MAX_PASSES] = {0, 0, 0};
     int gm = 0, gi = 0;
+    int tpb = 1;  // threads per radix-4 butterfly in every kernel of the step
 };
 static std::map<std::pair<int, int>, Shape> g_tuned;  // (lg, mode) -> autotuned shape
 
@@ -275,6 +276,7 @@ struct Pool {
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (base, count) -> GSTEPS-step graph
     bool big = false;
     int gm[2] = {2, 2}, gi[2] = {2, 2};  // middle / inner columns per CTA: [0] one residue per launch, [1] many
+    int tpb[2] = {1, 1};                 // threads per radix-4 butterfly (2: paired lanes)
     bool capturing = false;
     GridBar* bar = nullptr;      // grid barrier of the persistent kernel
     int persist_grid = 0;        // co-resident CTAs for it (0: not available)
@@ -312,12 +314,16 @@ static void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream
 }
 
 template <int F0>
-static void launch_first(dim3 g, cudaStream_t s, const Slot* sl, int base, const PlanDev& pd, const Slot& one) {
-    launch_pdl(k_first<F0>, g, dim3(2 * F0), s, sl, base, pd, one);
+static void launch_first(int tpb, dim3 g, cudaStream_t s, const Slot* sl, int base, const PlanDev& pd,
+                         const Slot& one) {
+    if (tpb == 2) launch_pdl(k_first<F0, 2>, g, dim3(4 * F0), s, sl, base, pd, one);
+    else launch_pdl(k_first<F0, 1>, g, dim3(2 * F0), s, sl, base, pd, one);
 }
 template <int F0>
-static void launch_last(dim3 g, cudaStream_t s, const Slot* sl, int base, const PlanDev& pd, const Slot& one) {
-    launch_pdl(k_last<F0>, g, dim3(2 * F0), s, sl, base, pd, one);
+static void launch_last(int tpb, dim3 g, cudaStream_t s, const Slot* sl, int base, const PlanDev& pd,
+                        const Slot& one) {
+    if (tpb == 2) launch_pdl(k_last<F0, 2>, g, dim3(4 * F0), s, sl, base, pd, one);
+    else launch_pdl(k_last<F0, 1>, g, dim3(2 * F0), s, sl, base, pd, one);
 }
 
 static int enqueue_step_part(Pool* p, int part, int base, int count, bool solo = false);
@@ -343,41 +349,46 @@ static int enqueue_step_part(Pool* p, int part, int base, int count, bool solo) 
     memset(&one, 0, sizeof(one));
     if (solo) one = p->hslots[base];
     const dim3 g0(d.S[0] / RUN, count);
-    const int Gm = p->gm[count == 1 ? 0 : 1];
-    const int Gi = p->gi[count == 1 ? 0 : 1];
+    const int mode = count == 1 ? 0 : 1;
+    const int Gm = p->gm[mode];
+    const int Gi = p->gi[mode];
+    const int T = p->tpb[mode];
     const int Fl = d.F[d.P - 1];
     int nl = 0;
     if (part == 0) {
         switch (d.F[0]) {
-            case 16: launch_first<16>(g0, p->stream, p->dslots, base, d, one); break;
-            case 32: launch_first<32>(g0, p->stream, p->dslots, base, d, one); break;
-            case 64: launch_first<64>(g0, p->stream, p->dslots, base, d, one); break;
-            case 128: launch_first<128>(g0, p->stream, p->dslots, base, d, one); break;
+            case 16: launch_first<16>(T, g0, p->stream, p->dslots, base, d, one); break;
+            case 32: launch_first<32>(T, g0, p->stream, p->dslots, base, d, one); break;
+            case 64: launch_first<64>(T, g0, p->stream, p->dslots, base, d, one); break;
+            case 128: launch_first<128>(T, g0, p->stream, p->dslots, base, d, one); break;
         }
     } else if (part == parts - 1) {
         switch (d.F[0]) {
-            case 16: launch_last<16>(g0, p->stream, p->dslots, base, d, one); break;
-            case 32: launch_last<32>(g0, p->stream, p->dslots, base, d, one); break;
-            case 64: launch_last<64>(g0, p->stream, p->dslots, base, d, one); break;
-            case 128: launch_last<128>(g0, p->stream, p->dslots, base, d, one); break;
+            case 16: launch_last<16>(T, g0, p->stream, p->dslots, base, d, one); break;
+            case 32: launch_last<32>(T, g0, p->stream, p->dslots, base, d, one); break;
+            case 64: launch_last<64>(T, g0, p->stream, p->dslots, base, d, one); break;
+            case 128: launch_last<128>(T, g0, p->stream, p->dslots, base, d, one); break;
         }
     } else if ((d.P == 3 && part == 2) || (d.P == 2 && part == 1)) {
         const dim3 gi(d.M / (Fl * Gi), count);
-#define PG_INNER2(FF, GG, LP) \
-    if (Fl == FF && Gi == GG && d.P - 1 == LP && ++nl) launch_pdl(k_inner<FF, GG, LP>, gi, dim3(FF * GG / 4), p->stream, (const Slot*)p->dslots, base, d, one);
-        PG_INNER2(16, 8, 1) PG_INNER2(32, 4, 1) PG_INNER2(32, 8, 1) PG_INNER2(64, 2, 1) PG_INNER2(64, 8, 1)
-        PG_INNER2(128, 2, 1) PG_INNER2(128, 4, 1)
-        PG_INNER2(32, 4, 2) PG_INNER2(32, 8, 2) PG_INNER2(64, 2, 2) PG_INNER2(64, 8, 2)
+#define PG_INNER2(FF, GG, LP, TT) \
+    if (Fl == FF && Gi == GG && d.P - 1 == LP && T == TT && ++nl) launch_pdl(k_inner<FF, GG, LP, TT>, gi, dim3(FF * GG / 4 * TT), p->stream, (const Slot*)p->dslots, base, d, one);
+        PG_INNER2(16, 8, 1, 1) PG_INNER2(32, 4, 1, 1) PG_INNER2(32, 8, 1, 1) PG_INNER2(64, 2, 1, 1)
+        PG_INNER2(64, 8, 1, 1) PG_INNER2(128, 2, 1, 1) PG_INNER2(128, 4, 1, 1)
+        PG_INNER2(32, 4, 2, 1) PG_INNER2(32, 8, 2, 1) PG_INNER2(64, 2, 2, 1) PG_INNER2(64, 8, 2, 1)
+        PG_INNER2(16, 8, 1, 2) PG_INNER2(32, 4, 1, 2) PG_INNER2(64, 2, 1, 2) PG_INNER2(128, 2, 1, 2)
+        PG_INNER2(32, 4, 2, 2) PG_INNER2(64, 2, 2, 2)
 #undef PG_INNER2
     } else {
         if (d.P != 3) return PG_EINVAL;
         const dim3 gm(d.M / (d.F[1] * Gm), count);
-#define PG_MID2(FF, GG)                                                                            \
-    if (d.F[1] == FF && Gm == GG && ++nl) {                                                       \
-        if (part == 1) launch_pdl(k_mid_fwd<FF, GG>, gm, dim3(FF * GG / 4), p->stream, (const Slot*)p->dslots, base, d, one); \
-        else launch_pdl(k_mid_inv<FF, GG>, gm, dim3(FF * GG / 4), p->stream, (const Slot*)p->dslots, base, d, one);         \
+#define PG_MID2(FF, GG, TT)                                                                        \
+    if (d.F[1] == FF && Gm == GG && T == TT && ++nl) {                                            \
+        if (part == 1) launch_pdl(k_mid_fwd<FF, GG, TT>, gm, dim3(FF * GG / 4 * TT), p->stream, (const Slot*)p->dslots, base, d, one); \
+        else launch_pdl(k_mid_inv<FF, GG, TT>, gm, dim3(FF * GG / 4 * TT), p->stream, (const Slot*)p->dslots, base, d, one);         \
     }
-        PG_MID2(32, 2) PG_MID2(32, 8) PG_MID2(64, 2) PG_MID2(64, 8)
+        PG_MID2(32, 2, 1) PG_MID2(32, 8, 1) PG_MID2(64, 2, 1) PG_MID2(64, 8, 1)
+        PG_MID2(32, 2, 2) PG_MID2(64, 2, 2)
 #undef PG_MID2
     }
     if (part != 0 && part != parts - 1 && nl != 1) return PG_EINVAL;  // no kernel instance for this shape
@@ -440,6 +451,7 @@ static int pool_create(int lg, int S, Pool** out, int mode = 0, const Shape* sha
     if (have && shape) {
         p->gm[0] = p->gm[1] = sh.gm;
         p->gi[0] = p->gi[1] = sh.gi;
+        p->tpb[0] = p->tpb[1] = sh.tpb;
     } else {
         std::lock_guard<std::mutex> lk(g_cache_mu);
         for (int m = 0; m < 2; ++m) {
@@ -450,6 +462,7 @@ static int pool_create(int lg, int S, Pool** out, int mode = 0, const Shape* sha
                 t.F[2] == plan->dev.F[2]) {
                 p->gm[m] = t.gm;
                 p->gi[m] = t.gi;
+                p->tpb[m] = t.tpb;
             }
         }
     }

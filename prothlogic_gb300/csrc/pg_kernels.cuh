@@ -121,14 +121,85 @@ __device__ __forceinline__ int tix(int g, int i) {
     return GROUP_MAJOR ? g * F + i : i * G + g;
 }
 
+// Radix-4 stage s of the forward transform done by a PAIR of adjacent lanes:
+// lane `sub` of the pair holds inputs sub and sub+2 of the butterfly, forms
+// their sum and difference, swaps one of them with its partner (shuffle), and
+// produces outputs sub and sub+2 with their twiddles.  The operations and their
+// order are those of bfly4_fwd + cmul, so the results are bit-identical to the
+// one-thread butterfly; each lane's FP64 chain is 16 instructions instead of 28,
+// at the price of a multiplication by w^0 = 1 (exact) on lane 0.
+template <int F, int G, bool GM>
+__device__ __forceinline__ void pair_stage_fwd(double2* tile, const double2* __restrict__ wF, int tid, int s) {
+    const int sub = tid & 1;
+    const int b = tid >> 1;
+    const int g = b / (F / 4), w = b % (F / 4);
+    const int h = F >> (2 * (s + 1));
+    const int step = F / (4 * h);
+    const int blk = w / h, j = w % h;
+    const int i0 = blk * 4 * h + j;
+    const int ia = tix<F, G, GM>(g, i0 + sub * h), ib = tix<F, G, GM>(g, i0 + (sub + 2) * h);
+    const double2 xa = tile[ia], xb = tile[ib];
+    const double2 p = make_double2(xa.x + xb.x, xa.y + xb.y);
+    const double2 m = make_double2(xa.x - xb.x, xa.y - xb.y);
+    const double2 snd = sub ? p : m;
+    const double2 rcv = make_double2(__shfl_xor_sync(0xffffffffu, snd.x, 1), __shfl_xor_sync(0xffffffffu, snd.y, 1));
+    const double2 u = sub ? rcv : p;                          // t0 | t1
+    const double2 v = sub ? make_double2(m.y, -m.x) : rcv;    // t2 | -i t3
+    double2 oa = make_double2(u.x + v.x, u.y + v.y);          // y0 | y1
+    double2 ob = make_double2(u.x - v.x, u.y - v.y);          // y2 | y3
+    if (h > 1) {
+        const int e = j * step;
+        oa = cmul(oa, wF[sub * e]);
+        ob = cmul(ob, wF[(2 + sub) * e]);
+    }
+    tile[ia] = oa;
+    tile[ib] = ob;
+}
+
+// Inverse counterpart (twiddles on the inputs, then bfly4_inv), bit-identical
+// to the one-thread butterfly.
+template <int F, int G, bool GM>
+__device__ __forceinline__ void pair_stage_inv(double2* tile, const double2* __restrict__ wF, int tid, int s) {
+    const int sub = tid & 1;
+    const int b = tid >> 1;
+    const int g = b / (F / 4), w = b % (F / 4);
+    const int h = F >> (2 * (s + 1));
+    const int step = F / (4 * h);
+    const int blk = w / h, j = w % h;
+    const int i0 = blk * 4 * h + j;
+    const int ia = tix<F, G, GM>(g, i0 + sub * h), ib = tix<F, G, GM>(g, i0 + (sub + 2) * h);
+    double2 za = tile[ia], zb = tile[ib];
+    if (h > 1) {
+        const int e = j * step;
+        za = cmulc(za, wF[sub * e]);
+        zb = cmulc(zb, wF[(2 + sub) * e]);
+    }
+    const double2 p = make_double2(za.x + zb.x, za.y + zb.y);
+    const double2 m = make_double2(za.x - zb.x, za.y - zb.y);
+    const double2 snd = sub ? p : m;
+    const double2 rcv = make_double2(__shfl_xor_sync(0xffffffffu, snd.x, 1), __shfl_xor_sync(0xffffffffu, snd.y, 1));
+    const double2 u = sub ? rcv : p;                          // s | d
+    const double2 v = sub ? make_double2(-m.y, m.x) : rcv;    // t | i u
+    tile[ia] = make_double2(u.x + v.x, u.y + v.y);            // Z0 | Z1
+    tile[ib] = make_double2(u.x - v.x, u.y - v.y);            // Z2 | Z3
+}
+
 // In-place forward DFT of length F on G groups of a shared tile, NT threads.
 // Radix-4 stages with spans F/4, F/16, ...; a final radix-2 stage if log2 F is
 // odd.  Output order is the digit reversal that the host's permutation table
-// (plan construction) describes; the inverse below undoes it exactly.
+// (plan construction) describes; the inverse below undoes it exactly.  With
+// NT == F*G/2 every radix-4 butterfly is done by a pair of lanes.
 template <int F, int G, int NT, bool GM, class Sync>
 __device__ __forceinline__ void smem_fft_fwd(double2* tile, const double2* __restrict__ wF, int tid, Sync sync) {
     constexpr int LG = Lg<F>::v;
     constexpr int N4 = LG / 2;
+    if constexpr (NT == F * G / 2) {
+#pragma unroll
+        for (int s = 0; s < N4; ++s) {
+            pair_stage_fwd<F, G, GM>(tile, wF, tid, s);
+            sync();
+        }
+    } else {
 #pragma unroll
     for (int s = 0; s < N4; ++s) {
         const int h = F >> (2 * (s + 1));
@@ -154,6 +225,7 @@ __device__ __forceinline__ void smem_fft_fwd(double2* tile, const double2* __res
             tile[tix<F, G, GM>(g, i0 + 3 * h)] = a3;
         }
         sync();
+    }
     }
     if (LG & 1) {
         for (int b = tid; b < G * F / 2; b += NT) {
@@ -181,6 +253,14 @@ __device__ __forceinline__ void smem_fft_inv(double2* tile, const double2* __res
             tile[tix<F, G, GM>(g, i0 + 1)] = make_double2(a.x - c.x, a.y - c.y);
         }
         sync();
+    }
+    if constexpr (NT == F * G / 2) {
+#pragma unroll
+        for (int s = N4 - 1; s >= 0; --s) {
+            pair_stage_inv<F, G, GM>(tile, wF, tid, s);
+            sync();
+        }
+        return;
     }
 #pragma unroll
     for (int s = N4 - 1; s >= 0; --s) {
@@ -575,58 +655,82 @@ __device__ __forceinline__ void tile_last(const Slot& sl, const Slot& pb, const 
 // `one` (by value): when its digits pointer is set, the launch squares that
 // single residue (blockIdx.y == 0) for a step count the host controls exactly,
 // so the kernels skip the slot-table load and the activity checks.
+//
+// Each kernel copies the F roots of unity of its pass into shared memory before
+// it waits on the previous kernel, so the transform stages read them from
+// shared memory instead of paying a global-memory round trip inside the chain.
+// The tile functions sync before their first stage, which publishes the copy.
+template <int F>
+__device__ __forceinline__ const PlanDev roots_in_smem(const PlanDev& pl, int pass, double2* wsm) {
+    const double2* __restrict__ g = pl.wF[pass];
+    for (int i = threadIdx.x; i < F; i += blockDim.x) wsm[i] = g[i];
+    PlanDev p2 = pl;
+    p2.wF[pass] = wsm;
+    return p2;
+}
 
-template <int F0>
-__global__ void __launch_bounds__(2 * F0) k_first(const Slot* __restrict__ slots, int base, const PlanDev pl,
-                                                  const Slot one) {
+// TPB: threads per radix-4 butterfly (1, or 2 for the paired-lane transform).
+template <int F0, int TPB = 1>
+__global__ void __launch_bounds__(2 * F0 * TPB) k_first(const Slot* __restrict__ slots, int base, const PlanDev pl,
+                                                        const Slot one) {
     __shared__ double2 tile[F0 * RUN];
     __shared__ int dsm[F0 * RUN];
+    __shared__ double2 wsm[F0];
+    const PlanDev pw = roots_in_smem<F0>(pl, 0, wsm);
     if (one.digits) {
-        tile_first<F0, 2 * F0>(one, pl, blockIdx.x, threadIdx.x, tile, dsm, BlockSync(), PdlOnly());
+        tile_first<F0, 2 * F0 * TPB>(one, pw, blockIdx.x, threadIdx.x, tile, dsm, BlockSync(), PdlOnly());
     } else {
         const Slot sl = slots[base + blockIdx.y];
-        tile_first<F0, 2 * F0>(sl, pl, blockIdx.x, threadIdx.x, tile, dsm, BlockSync(),
+        tile_first<F0, 2 * F0 * TPB>(sl, pw, blockIdx.x, threadIdx.x, tile, dsm, BlockSync(),
                                PdlFirst{sl.st, blockIdx.x == 0 && threadIdx.x == 0});
     }
     pdl_trigger();
 }
 
-template <int F, int G>
-__global__ void __launch_bounds__(F * G / 4) k_mid_fwd(const Slot* __restrict__ slots, int base, const PlanDev pl,
-                                                       const Slot one) {
+template <int F, int G, int TPB = 1>
+__global__ void __launch_bounds__(F * G / 4 * TPB) k_mid_fwd(const Slot* __restrict__ slots, int base,
+                                                             const PlanDev pl, const Slot one) {
     __shared__ double2 tile[F * G];
+    __shared__ double2 wsm[F];
+    const PlanDev pw = roots_in_smem<F>(pl, 1, wsm);
     if (one.digits) {
-        tile_mid_fwd<F, G, F * G / 4>(one, pl, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlOnly());
+        tile_mid_fwd<F, G, F * G / 4 * TPB>(one, pw, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlOnly());
     } else {
         const Slot sl = slots[base + blockIdx.y];
-        tile_mid_fwd<F, G, F * G / 4>(sl, pl, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlActive{sl.st, false});
+        tile_mid_fwd<F, G, F * G / 4 * TPB>(sl, pw, blockIdx.x, threadIdx.x, tile, BlockSync(),
+                                            PdlActive{sl.st, false});
     }
     pdl_trigger();
 }
 
-template <int F, int G>
-__global__ void __launch_bounds__(F * G / 4) k_mid_inv(const Slot* __restrict__ slots, int base, const PlanDev pl,
-                                                       const Slot one) {
+template <int F, int G, int TPB = 1>
+__global__ void __launch_bounds__(F * G / 4 * TPB) k_mid_inv(const Slot* __restrict__ slots, int base,
+                                                             const PlanDev pl, const Slot one) {
     __shared__ double2 tile[F * G];
+    __shared__ double2 wsm[F];
+    const PlanDev pw = roots_in_smem<F>(pl, 1, wsm);
     if (one.digits) {
-        tile_mid_inv<F, G, F * G / 4>(one, pl, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlOnly());
+        tile_mid_inv<F, G, F * G / 4 * TPB>(one, pw, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlOnly());
     } else {
         const Slot sl = slots[base + blockIdx.y];
-        tile_mid_inv<F, G, F * G / 4>(sl, pl, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlActive{sl.st, true});
+        tile_mid_inv<F, G, F * G / 4 * TPB>(sl, pw, blockIdx.x, threadIdx.x, tile, BlockSync(),
+                                            PdlActive{sl.st, true});
     }
     pdl_trigger();
 }
 
-template <int F, int G, int LASTP>
-__global__ void __launch_bounds__(F * G / 4) k_inner(const Slot* __restrict__ slots, int base, const PlanDev pl,
-                                                     const Slot one) {
+template <int F, int G, int LASTP, int TPB = 1>
+__global__ void __launch_bounds__(F * G / 4 * TPB) k_inner(const Slot* __restrict__ slots, int base,
+                                                           const PlanDev pl, const Slot one) {
     __shared__ double2 tile[F * G];
     __shared__ double2 tile2[F * G];
+    __shared__ double2 wsm[F];
+    const PlanDev pw = roots_in_smem<F>(pl, LASTP, wsm);
     if (one.digits) {
         pdl_wait();
         if (blockIdx.x == 0 && threadIdx.x == 0) one.st->step += 1;
-        tile_inner<F, G, LASTP, F * G / 4>(one, one, true, pl, blockIdx.x, threadIdx.x, tile, tile2, BlockSync(),
-                                            NoWait());
+        tile_inner<F, G, LASTP, F * G / 4 * TPB>(one, one, true, pw, blockIdx.x, threadIdx.x, tile, tile2,
+                                                  BlockSync(), NoWait());
         pdl_trigger();
         return;
     }
@@ -638,25 +742,27 @@ __global__ void __launch_bounds__(F * G / 4) k_inner(const Slot* __restrict__ sl
     if (st->op == OP_FORWARD) return;                       // the partner's k_inner transforms this slot
     const int partner = st->partner;
     const bool square = partner == base + (int)blockIdx.y;
-    tile_inner<F, G, LASTP, F * G / 4>(sl, slots[partner], square, pl, blockIdx.x, threadIdx.x, tile, tile2,
-                                        BlockSync(), NoWait());
+    tile_inner<F, G, LASTP, F * G / 4 * TPB>(sl, slots[partner], square, pw, blockIdx.x, threadIdx.x, tile, tile2,
+                                              BlockSync(), NoWait());
     pdl_trigger();
 }
 
-template <int F0>
-__global__ void __launch_bounds__(2 * F0) k_last(const Slot* __restrict__ slots, int base, const PlanDev pl,
-                                                 const Slot one) {
+template <int F0, int TPB = 1>
+__global__ void __launch_bounds__(2 * F0 * TPB) k_last(const Slot* __restrict__ slots, int base, const PlanDev pl,
+                                                       const Slot one) {
     __shared__ double2 tile[F0 * RUN];
     __shared__ long long cl[F0 * RUN];
     __shared__ long long ch[F0 * RUN];
+    __shared__ double2 wsm[F0];
+    const PlanDev pw = roots_in_smem<F0>(pl, 0, wsm);
     if (one.digits) {
-        tile_last<F0, 2 * F0>(one, one, pl, blockIdx.x, threadIdx.x, tile, cl, ch, BlockSync(), PdlOnly());
+        tile_last<F0, 2 * F0 * TPB>(one, one, pw, blockIdx.x, threadIdx.x, tile, cl, ch, BlockSync(), PdlOnly());
     } else {
         const Slot sl = slots[base + blockIdx.y];
         SlotState* st = sl.st;
         // the partner index is fixed by the host before the step: safe to read early
-        tile_last<F0, 2 * F0>(sl, slots[st->partner], pl, blockIdx.x, threadIdx.x, tile, cl, ch, BlockSync(),
-                              PdlActive{st, true});
+        tile_last<F0, 2 * F0 * TPB>(sl, slots[st->partner], pw, blockIdx.x, threadIdx.x, tile, cl, ch, BlockSync(),
+                                    PdlActive{st, true});
     }
     pdl_trigger();
 }

@@ -88,6 +88,6 @@ def test_tuned_batch_full_tests_exact(pg, gmp):
 
 
 def test_tune_set_rejects_shapes_that_are_not_compiled(pg):
-    bad = {"lg": 12, "slots": 1, "passes": 2, "f0": 16, "f1": 256, "f2": 0, "g_mid": 2, "g_inner": 2}
+    bad = {"lg": 12, "slots": 1, "passes": 2, "f0": 16, "f1": 256, "f2": 0, "g_mid": 2, "g_inner": 2, "tpb": 1}
     with pytest.raises(pg.ProthGpuError):
         pg.tune_set(pg.TUNE_ONE, bad)
