@@ -655,19 +655,6 @@ __device__ __forceinline__ void tile_last(const Slot& sl, const Slot& pb, const 
 // `one` (by value): when its digits pointer is set, the launch squares that
 // single residue (blockIdx.y == 0) for a step count the host controls exactly,
 // so the kernels skip the slot-table load and the activity checks.
-//
-// Each kernel copies the F roots of unity of its pass into shared memory before
-// it waits on the previous kernel, so the transform stages read them from
-// shared memory instead of paying a global-memory round trip inside the chain.
-// The tile functions sync before their first stage, which publishes the copy.
-template <int F>
-__device__ __forceinline__ const PlanDev roots_in_smem(const PlanDev& pl, int pass, double2* wsm) {
-    const double2* __restrict__ g = pl.wF[pass];
-    for (int i = threadIdx.x; i < F; i += blockDim.x) wsm[i] = g[i];
-    PlanDev p2 = pl;
-    p2.wF[pass] = wsm;
-    return p2;
-}
 
 // TPB: threads per radix-4 butterfly (1, or 2 for the paired-lane transform).
 template <int F0, int TPB = 1>
@@ -675,13 +662,11 @@ __global__ void __launch_bounds__(2 * F0 * TPB) k_first(const Slot* __restrict__
                                                         const Slot one) {
     __shared__ double2 tile[F0 * RUN];
     __shared__ int dsm[F0 * RUN];
-    __shared__ double2 wsm[F0];
-    const PlanDev pw = roots_in_smem<F0>(pl, 0, wsm);
     if (one.digits) {
-        tile_first<F0, 2 * F0 * TPB>(one, pw, blockIdx.x, threadIdx.x, tile, dsm, BlockSync(), PdlOnly());
+        tile_first<F0, 2 * F0 * TPB>(one, pl, blockIdx.x, threadIdx.x, tile, dsm, BlockSync(), PdlOnly());
     } else {
         const Slot sl = slots[base + blockIdx.y];
-        tile_first<F0, 2 * F0 * TPB>(sl, pw, blockIdx.x, threadIdx.x, tile, dsm, BlockSync(),
+        tile_first<F0, 2 * F0 * TPB>(sl, pl, blockIdx.x, threadIdx.x, tile, dsm, BlockSync(),
                                PdlFirst{sl.st, blockIdx.x == 0 && threadIdx.x == 0});
     }
     pdl_trigger();
@@ -691,13 +676,11 @@ template <int F, int G, int TPB = 1>
 __global__ void __launch_bounds__(F * G / 4 * TPB) k_mid_fwd(const Slot* __restrict__ slots, int base,
                                                              const PlanDev pl, const Slot one) {
     __shared__ double2 tile[F * G];
-    __shared__ double2 wsm[F];
-    const PlanDev pw = roots_in_smem<F>(pl, 1, wsm);
     if (one.digits) {
-        tile_mid_fwd<F, G, F * G / 4 * TPB>(one, pw, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlOnly());
+        tile_mid_fwd<F, G, F * G / 4 * TPB>(one, pl, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlOnly());
     } else {
         const Slot sl = slots[base + blockIdx.y];
-        tile_mid_fwd<F, G, F * G / 4 * TPB>(sl, pw, blockIdx.x, threadIdx.x, tile, BlockSync(),
+        tile_mid_fwd<F, G, F * G / 4 * TPB>(sl, pl, blockIdx.x, threadIdx.x, tile, BlockSync(),
                                             PdlActive{sl.st, false});
     }
     pdl_trigger();
@@ -707,13 +690,11 @@ template <int F, int G, int TPB = 1>
 __global__ void __launch_bounds__(F * G / 4 * TPB) k_mid_inv(const Slot* __restrict__ slots, int base,
                                                              const PlanDev pl, const Slot one) {
     __shared__ double2 tile[F * G];
-    __shared__ double2 wsm[F];
-    const PlanDev pw = roots_in_smem<F>(pl, 1, wsm);
     if (one.digits) {
-        tile_mid_inv<F, G, F * G / 4 * TPB>(one, pw, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlOnly());
+        tile_mid_inv<F, G, F * G / 4 * TPB>(one, pl, blockIdx.x, threadIdx.x, tile, BlockSync(), PdlOnly());
     } else {
         const Slot sl = slots[base + blockIdx.y];
-        tile_mid_inv<F, G, F * G / 4 * TPB>(sl, pw, blockIdx.x, threadIdx.x, tile, BlockSync(),
+        tile_mid_inv<F, G, F * G / 4 * TPB>(sl, pl, blockIdx.x, threadIdx.x, tile, BlockSync(),
                                             PdlActive{sl.st, true});
     }
     pdl_trigger();
@@ -724,12 +705,10 @@ __global__ void __launch_bounds__(F * G / 4 * TPB) k_inner(const Slot* __restric
                                                            const PlanDev pl, const Slot one) {
     __shared__ double2 tile[F * G];
     __shared__ double2 tile2[F * G];
-    __shared__ double2 wsm[F];
-    const PlanDev pw = roots_in_smem<F>(pl, LASTP, wsm);
     if (one.digits) {
         pdl_wait();
         if (blockIdx.x == 0 && threadIdx.x == 0) one.st->step += 1;
-        tile_inner<F, G, LASTP, F * G / 4 * TPB>(one, one, true, pw, blockIdx.x, threadIdx.x, tile, tile2,
+        tile_inner<F, G, LASTP, F * G / 4 * TPB>(one, one, true, pl, blockIdx.x, threadIdx.x, tile, tile2,
                                                   BlockSync(), NoWait());
         pdl_trigger();
         return;
@@ -742,7 +721,7 @@ __global__ void __launch_bounds__(F * G / 4 * TPB) k_inner(const Slot* __restric
     if (st->op == OP_FORWARD) return;                       // the partner's k_inner transforms this slot
     const int partner = st->partner;
     const bool square = partner == base + (int)blockIdx.y;
-    tile_inner<F, G, LASTP, F * G / 4 * TPB>(sl, slots[partner], square, pw, blockIdx.x, threadIdx.x, tile, tile2,
+    tile_inner<F, G, LASTP, F * G / 4 * TPB>(sl, slots[partner], square, pl, blockIdx.x, threadIdx.x, tile, tile2,
                                               BlockSync(), NoWait());
     pdl_trigger();
 }
@@ -753,15 +732,13 @@ __global__ void __launch_bounds__(2 * F0 * TPB) k_last(const Slot* __restrict__ 
     __shared__ double2 tile[F0 * RUN];
     __shared__ long long cl[F0 * RUN];
     __shared__ long long ch[F0 * RUN];
-    __shared__ double2 wsm[F0];
-    const PlanDev pw = roots_in_smem<F0>(pl, 0, wsm);
     if (one.digits) {
-        tile_last<F0, 2 * F0 * TPB>(one, one, pw, blockIdx.x, threadIdx.x, tile, cl, ch, BlockSync(), PdlOnly());
+        tile_last<F0, 2 * F0 * TPB>(one, one, pl, blockIdx.x, threadIdx.x, tile, cl, ch, BlockSync(), PdlOnly());
     } else {
         const Slot sl = slots[base + blockIdx.y];
         SlotState* st = sl.st;
         // the partner index is fixed by the host before the step: safe to read early
-        tile_last<F0, 2 * F0 * TPB>(sl, slots[st->partner], pw, blockIdx.x, threadIdx.x, tile, cl, ch, BlockSync(),
+        tile_last<F0, 2 * F0 * TPB>(sl, slots[st->partner], pl, blockIdx.x, threadIdx.x, tile, cl, ch, BlockSync(),
                                     PdlActive{st, true});
     }
     pdl_trigger();
