@@ -384,6 +384,14 @@ def run_gpu(args, world, rank, local, pgd):
     stats = eng.stats()
     res = eng.get_residue()
     max_err = eng.max_err()
+    # per-kernel device times of one squaring, kernels launched one by one with
+    # events around each (untimed; serialised like the ncu launch list, so the
+    # shares compare with profiles/squaring_n1048576.md)
+    prof = [eng.profile_step() for _ in range(20)]
+    names = ["k_first", "k_mid_fwd", "k_inner", "k_mid_inv", "k_last"] if len(prof[0]) == 5 else \
+        ["k_first", "k_inner", "k_last"]
+    per_k = [statistics.median(p[i] for p in prof) * 1e3 for i in range(len(names))]
+    kernels_live = [{"kernel": nm, "us": t, "share": t / sum(per_k)} for nm, t in zip(names, per_k)]
     value = total_ms * 1e6 / (K * SQ_PER_STEP * world)
 
     # parity of the timed run: RES64 after K*1000 squarings of x0 = a (GMP values)
@@ -443,6 +451,7 @@ def run_gpu(args, world, rank, local, pgd):
                    "fft_bumps": stats["fft_bumps"], "max_err": max_err, "shape": _chosen(tune_rows)},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved_gbs / hbm_peak if hbm_peak else None, "traffic": traffic,
+                     "kernels_live": kernels_live,
                      "note": "measured hbm_gbs peak; unit = one squaring (its 5 kernels); traffic = DRAM "
                              "bytes of those 5 launches under ncu (cold caches; L2-resident in steady "
                              "state); the real bound is the FP64 pipe, see roofline_fp64"},
@@ -490,6 +499,18 @@ def uneven_full():
     return 0
 
 
+def ncu_batch_target():
+    """Small profiling target for the batched path: 256 candidates at n = 65536, 100 steps."""
+    import prothlogic_gb300 as pg
+    b = pg.Batch(256)
+    for i, (k, n) in enumerate(workloads.uniform(count=256)):
+        b.submit(k, n, i)
+    b.run(100)
+    print("pending", b.pending())
+    b.close()
+    return 0
+
+
 def ncu_target():
     """Small profiling target: one n = 1,048,576 residue, 200 squarings, no Gerbicz."""
     import prothlogic_gb300 as pg
@@ -510,9 +531,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ncu-target", action="store_true", help="run only the small profiling target")
     ap.add_argument("--uneven-full", action="store_true", help="run the whole uneven batch to completion")
+    ap.add_argument("--ncu-batch-target", action="store_true", help="run only the small batched profiling target")
     args = ap.parse_args()
     if args.ncu_target:
         return ncu_target()
+    if args.ncu_batch_target:
+        return ncu_batch_target()
     if args.uneven_full:
         return uneven_full()
     if args.warmup < 3:

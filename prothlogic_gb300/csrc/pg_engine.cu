@@ -273,6 +273,7 @@ struct Pool {
     long long* h_rb_top = nullptr;
     SlotState* h_st = nullptr;  // pinned mirror
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;  // second chain of an engine (created on first use)
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (base, count) -> GSTEPS-step graph
     bool big = false;
     int gm[2] = {2, 2}, gi[2] = {2, 2};  // middle / inner columns per CTA: [0] one residue per launch, [1] many
@@ -414,6 +415,7 @@ static void pool_free(Pool* p) {
     cudaFreeHost(p->h_rb_top);
     cudaFreeHost(p->h_st);
     if (p->stream) cudaStreamDestroy(p->stream);
+    if (p->stream2) cudaStreamDestroy(p->stream2);
     delete p;
 }
 
@@ -667,6 +669,72 @@ static int pool_run(Pool* p, long long steps, bool use_graph, int base = 0, int 
     return PG_OK;
 }
 
+// Graph of GSTEPS solo steps of slot `base` (captured on the pool stream on first use).
+static int solo_graph(Pool* p, int base, cudaGraphExec_t* out) {
+    const auto key = std::make_pair(-1 - base, 1);
+    auto it = p->graphs.find(key);
+    if (it != p->graphs.end()) {
+        *out = it->second;
+        return PG_OK;
+    }
+    cudaGraph_t g;
+    PG_CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = PG_OK;
+    p->capturing = true;
+    for (int i = 0; i < GSTEPS && rc == PG_OK; ++i) rc = enqueue_step(p, base, 1, true);
+    p->capturing = false;
+    cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
+    if (rc) return rc;
+    PG_CK(ce);
+    cudaGraphExec_t ge;
+    PG_CK(cudaGraphInstantiate(&ge, g, 0));
+    cudaGraphDestroy(g);
+    p->graphs[key] = ge;
+    *out = ge;
+    return PG_OK;
+}
+
+// `steps` squarings of slots a and a+1 as two independent solo chains, a on the
+// pool stream and a+1 on a second stream, so that the two latency-bound chains
+// overlap on the GPU instead of sharing one launch (used for the Gerbicz
+// verification chain beside the residue).  Returns with the pool stream
+// ordered after both chains.
+static int pool_run_pair(Pool* p, long long steps, int a) {
+    if (!p->stream2) PG_CK(cudaStreamCreateWithFlags(&p->stream2, cudaStreamNonBlocking));
+    cudaGraphExec_t ga = nullptr, gb = nullptr;
+    if (steps >= GSTEPS) {
+        int rc = solo_graph(p, a, &ga);
+        if (!rc) rc = solo_graph(p, a + 1, &gb);
+        if (rc) return rc;
+    }
+    cudaEvent_t fork, join;
+    PG_CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    PG_CK(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+    PG_CK(cudaEventRecord(fork, p->stream));
+    PG_CK(cudaStreamWaitEvent(p->stream2, fork, 0));
+    int rc = PG_OK;
+    const int parts = p->plan->dev.P == 3 ? 5 : 3;
+    while (steps > 0 && rc == PG_OK) {
+        if (ga && steps >= GSTEPS) {
+            if (cudaGraphLaunch(ga, p->stream) != cudaSuccess || cudaGraphLaunch(gb, p->stream2) != cudaSuccess)
+                rc = PG_ECUDA;
+            g_launches += 2ull * GSTEPS * parts;
+            steps -= GSTEPS;
+        } else {
+            rc = enqueue_step(p, a, 1, true);
+            std::swap(p->stream, p->stream2);  // the second chain's step goes to the second stream
+            if (!rc) rc = enqueue_step(p, a + 1, 1, true);
+            std::swap(p->stream, p->stream2);
+            steps -= 1;
+        }
+    }
+    cudaEventRecord(join, p->stream2);
+    cudaStreamWaitEvent(p->stream, join, 0);
+    cudaEventDestroy(fork);
+    cudaEventDestroy(join);
+    return rc;
+}
+
 static double bits_to_double(unsigned long long b) {
     double d;
     memcpy(&d, &b, sizeof(d));
@@ -870,6 +938,8 @@ static int run_squarings(pg_engine* e, int s, uint64_t steps, int count = 1) {
                 PG_CK(cudaStreamSynchronize(e->pool->stream));
                 continue;
             }
+        } else if (count == 2 && !(e->flags & PG_FLAG_NO_GRAPH)) {
+            rc = pool_run_pair(e->pool, (long long)c, s);
         } else {
             rc = pool_run(e->pool, (long long)c, !(e->flags & PG_FLAG_NO_GRAPH), s, count, count == 1);
         }
