@@ -45,7 +45,7 @@ enum SlotOp : int {
     OP_FORWARD = 1   // operand of another slot's product: fix up + forward passes only
 };
 
-enum SlotFlags : int { SF_DIGIT_OVERFLOW = 1, SF_ROUND_RANGE = 2 };
+enum SlotFlags : int { SF_DIGIT_OVERFLOW = 1, SF_ROUND_RANGE = 2, SF_WAIT_TIMEOUT = 4 };
 
 // Per-slot descriptor (device memory, read-only during a step).
 struct Slot {

@@ -260,8 +260,7 @@ __device__ __forceinline__ void smem_fft_inv(double2* tile, const double2* __res
             pair_stage_inv<F, G, GM>(tile, wF, tid, s);
             sync();
         }
-        return;
-    }
+    } else {
 #pragma unroll
     for (int s = N4 - 1; s >= 0; --s) {
         const int h = F >> (2 * (s + 1));
@@ -287,6 +286,7 @@ __device__ __forceinline__ void smem_fft_inv(double2* tile, const double2* __res
             tile[tix<F, G, GM>(g, i0 + 3 * h)] = z3;
         }
         sync();
+    }
     }
 }
 
@@ -562,6 +562,88 @@ __device__ __forceinline__ void tile_inner(const Slot& sl, const Slot& pb, bool 
     for (int e = tid; e < F * G; e += NT) bp[e] = tile[e];
 }
 
+// ---- bulk asynchronous copies (the TMA engine's non-tensor form) ----
+// The last pass's tile is F*G contiguous complex values of one slot's spectrum,
+// so one thread moves it between global and shared memory with a single bulk
+// copy, completed through an mbarrier, instead of every thread issuing loads.
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// Wait for phase `parity` of the barrier, at most kMbarPolls polls; false if it
+// did not complete.
+constexpr int kMbarPolls = 1 << 22;
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    for (int i = 0; i < kMbarPolls; ++i) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void bulk_store(void* dst, const void* src, unsigned bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+// tile_inner with the tile (and the partner's tile) brought in and written back
+// by bulk copies.  `bar` is an initialised barrier of this CTA (phase 0 unused).
+// If the load does not complete within the poll limit, the slot is flagged, the
+// copy is waited for once more, and the tile is left alone.
+template <int F, int G, int LASTP, int NT, class Sync>
+__device__ __forceinline__ void tile_inner_bulk(const Slot& sl, const Slot& pb, bool square, const PlanDev& pl,
+                                                int cta, int tid, double2* tile, double2* tile2,
+                                                unsigned long long* bar, Sync sync) {
+    constexpr unsigned BYTES = F * G * sizeof(double2);
+    double2* bp = sl.spec + (size_t)cta * (F * G);
+    if (tid == 0) {
+        mbar_expect_tx(bar, square ? BYTES : 2 * BYTES);
+        bulk_load(tile, bp, BYTES, bar);
+        if (!square) bulk_load(tile2, pb.spec + (size_t)cta * (F * G), BYTES, bar);
+    }
+    if (!mbar_wait(bar, 0)) {
+        if (tid == 0) atomicOr(&sl.st->flags, SF_WAIT_TIMEOUT);
+        mbar_wait(bar, 0);
+        return;
+    }
+    smem_fft_fwd<F, G, NT, true>(tile, pl.wF[LASTP], tid, sync);
+    if (square) {
+        for (int e = tid; e < F * G; e += NT) {
+            const double2 z = tile[e];
+            tile[e] = make_double2(fma(z.x, z.x, -(z.y * z.y)), (z.x + z.x) * z.y);
+        }
+    } else {
+        smem_fft_fwd<F, G, NT, true>(tile2, pl.wF[LASTP], tid, sync);
+        for (int e = tid; e < F * G; e += NT) tile[e] = cmul(tile[e], tile2[e]);
+    }
+    sync();
+    smem_fft_inv<F, G, NT, true>(tile, pl.wF[LASTP], tid, sync);
+    // the inverse ends with a barrier after its last stage; make the generic-proxy
+    // writes visible to the bulk copy, then one thread stores the tile
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    sync();
+    if (tid == 0) bulk_store(bp, tile, BYTES);
+}
+
 // Pass 0 inverse + unweight + round (max |err|) + Montgomery fold + in-run carry.
 template <int F0, int NT, class Sync, class Pre>
 __device__ __forceinline__ void tile_last(const Slot& sl, const Slot& pb, const PlanDev& pl, int cta, int tid,
@@ -703,13 +785,16 @@ __global__ void __launch_bounds__(F * G / 4 * TPB) k_mid_inv(const Slot* __restr
 template <int F, int G, int LASTP, int TPB = 1>
 __global__ void __launch_bounds__(F * G / 4 * TPB) k_inner(const Slot* __restrict__ slots, int base,
                                                            const PlanDev pl, const Slot one) {
-    __shared__ double2 tile[F * G];
-    __shared__ double2 tile2[F * G];
+    __shared__ __align__(128) double2 tile[F * G];
+    __shared__ __align__(128) double2 tile2[F * G];
+    __shared__ unsigned long long bar;
+    if (threadIdx.x == 0) mbar_init(&bar);
+    __syncthreads();
     if (one.digits) {
         pdl_wait();
         if (blockIdx.x == 0 && threadIdx.x == 0) one.st->step += 1;
-        tile_inner<F, G, LASTP, F * G / 4 * TPB>(one, one, true, pl, blockIdx.x, threadIdx.x, tile, tile2,
-                                                  BlockSync(), NoWait());
+        tile_inner_bulk<F, G, LASTP, F * G / 4 * TPB>(one, one, true, pl, blockIdx.x, threadIdx.x, tile, tile2, &bar,
+                                                       BlockSync());
         pdl_trigger();
         return;
     }
@@ -721,8 +806,8 @@ __global__ void __launch_bounds__(F * G / 4 * TPB) k_inner(const Slot* __restric
     if (st->op == OP_FORWARD) return;                       // the partner's k_inner transforms this slot
     const int partner = st->partner;
     const bool square = partner == base + (int)blockIdx.y;
-    tile_inner<F, G, LASTP, F * G / 4 * TPB>(sl, slots[partner], square, pl, blockIdx.x, threadIdx.x, tile, tile2,
-                                              BlockSync(), NoWait());
+    tile_inner_bulk<F, G, LASTP, F * G / 4 * TPB>(sl, slots[partner], square, pl, blockIdx.x, threadIdx.x, tile,
+                                                   tile2, &bar, BlockSync());
     pdl_trigger();
 }
 
