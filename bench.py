@@ -232,6 +232,9 @@ def _chosen_radices(rows):
     return tuple(r[f] for f in ("f0", "f1", "f2")[: r["passes"]])
 
 
+GZ_EXTRA = 1500  # squarings per test spent on its end-of-chain Gerbicz check (1000 + 500 on average)
+
+
 def cpu_tests_per_hour(cands, sq_sample, budget_s=None):
     """Reference-algorithm tests/hour on all host cores (one test per thread, as the
     reference's dispatcher runs them, prothlogic4.2/dcore.cpp:125-188), from every
@@ -281,7 +284,7 @@ def uneven_sample(pg, steps=200, warm=50, cpu_sq=60):
         ms1, _ = e.time_squarings(500)
         e.close()
         one_sq = ms1 * 1e-3 / 500
-        work = sum(n - 1 + max(0, k.bit_length() - 1) for k, n in members)
+        work = sum(n - 1 + max(0, k.bit_length() - 1) + GZ_EXTRA for k, n in members)
         t_batch += work * per_cand_sq
         t_one += work * one_sq
         per_class[f"2^{lg}"] = {"candidates": len(members), "running": running,
@@ -321,7 +324,10 @@ def batched_sample(pg, steps=300, warm=60):
     admitted = running
     b.close()
     per_step_ms = ms / steps
-    sq_per_test = n - 1 + 19                # n-1 squarings + the a^k powering (bitlen(k) - 1 <= 19)
+    # n-1 squarings + the a^k powering (bitlen(k) - 1 <= 19) + the Gerbicz check at the
+    # end of each chain: one block (1000) of the product chain and on average half a
+    # block of tail recompute (the same allowance for the one-at-a-time engine)
+    sq_per_test = n - 1 + 19 + GZ_EXTRA
     tph_batch = admitted / (per_step_ms * 1e-3 * sq_per_test) * 3600.0
     # one candidate at a time on the whole GPU (same engine, FFT length 4096)
     k0 = cands[0][0]
@@ -344,7 +350,8 @@ def batched_sample(pg, steps=300, warm=60):
             "cpu_reference_tests_per_hour": cpu["tests_per_hour"],
             "batched_over_cpu": tph_batch / cpu["tests_per_hour"], "cpu": cpu,
             "sample": f"{steps} batch squaring steps after {warm} warm-up; one-at-a-time 2000 squarings; "
-                      "tests/hour extrapolated to n-1+19 squarings per test; no Gerbicz in either"}
+                      "tests/hour extrapolated to n-1+19 squarings per test plus 1,500 for the Gerbicz check "
+                      "(the CPU reference has none)"}
 
 
 def run_gpu(args, world, rank, local, pgd):

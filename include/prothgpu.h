@@ -192,8 +192,15 @@ int pg_batch_set_budget(pg_batch* b, uint64_t hbm_bytes);
 /* Test hook: add `delta` to digit `index` of the running candidate `tag`
  * (a simulated memory error; nothing faults).  PG_ESTATE if it is not running. */
 int pg_batch_debug_corrupt(pg_batch* b, uint64_t tag, uint32_t index, int32_t delta);
-/* Device bytes one candidate k*2^n+1 holds while admitted (slot + checkpoint). */
+/* Device bytes one candidate k*2^n+1 holds while admitted in a batch with the
+ * Gerbicz check (its five role slots, weights share, checkpoint copy). */
 uint64_t pg_slot_footprint(uint64_t k, uint32_t n);
+/* Gerbicz-Li block length (class steps) of a batch, before its first run
+ * (default 1000; the check is off with PG_FLAG_NO_GERBICZ at creation).  Each
+ * candidate is verified when its chain ends: one block of squarings of the
+ * product chain plus the tail since the last block end; a mismatch sends it
+ * back to its last verified residue.  pg_result reports checks and failures. */
+int pg_batch_set_gerbicz(pg_batch* b, uint64_t block);
 
 /* ---- launch-shape autotuner (replaces the reference's auto_tune_fft_len,
  * prothlogic4.2/dcore.cpp:20-81, which tunes only the FFT length) ----

@@ -106,6 +106,7 @@ SIGNATURES = {
     "pg_batch_set_budget": (ctypes.c_int, [_vp, _u64]),
     "pg_batch_debug_corrupt": (ctypes.c_int, [_vp, _u64, _u32, _i32]),
     "pg_slot_footprint": (_u64, [_u64, _u32]),
+    "pg_batch_set_gerbicz": (ctypes.c_int, [_vp, _u64]),
     "pg_autotune": (ctypes.c_int, [_u32, _u32, _u32, ctypes.POINTER(PgTuneResult), _sz, ctypes.POINTER(_sz)]),
     "pg_tune_get": (ctypes.c_int, [_u32, _u32, ctypes.POINTER(PgTuneResult)]),
     "pg_tune_set": (ctypes.c_int, [_u32, ctypes.POINTER(PgTuneResult)]),
@@ -360,6 +361,10 @@ class Batch:
 
     def run(self, max_steps=0):
         _check(load().pg_batch_run(self._h, max_steps), "pg_batch_run")
+
+    def set_gerbicz(self, block):
+        """Gerbicz block length in class steps (before the first run)."""
+        _check(load().pg_batch_set_gerbicz(self._h, block), "pg_batch_set_gerbicz")
 
     def run_timed(self, max_steps):
         """pg_batch_run with CUDA events on the class streams; returns device ms."""

@@ -397,3 +397,72 @@ def test_serving_loop_small(pg):
                 assert r["res64"] == y & M64
         else:
             assert N % r["factor"] == 0
+
+
+def _passing(seed, count, lo, hi, pg):
+    rng = random.Random(seed)
+    out = []
+    while len(out) < count:
+        k, n = 2 * rng.randrange(1, 5000) + 1, rng.randrange(lo, hi)
+        if not pg.gate_rejects(k, n) and pg.choose_base(k, n):
+            out.append((k, n))
+    return out
+
+
+def test_batch_gerbicz_clean_run(pg, gmp):
+    """Every batched candidate is Gerbicz-verified once at the end of its chain,
+    with no failure, and its residue is exact."""
+    cands = _passing(77, 4, 5200, 9000, pg)
+    b = pg.Batch(8)
+    b.set_gerbicz(1000)
+    for i, (k, n) in enumerate(cands):
+        b.submit(k, n, i)
+    b.run(0)
+    res = {r["tag"]: r for r in b.poll()}
+    assert len(res) == len(cands)
+    for i, (k, n) in enumerate(cands):
+        N = _N(k, n)
+        y = gmp.powmod(res[i]["base"], (N - 1) // 2, N)
+        assert res[i]["status"] == 0
+        assert res[i]["res64"] == y & M64 and res[i]["verdict"] == (y == N - 1)
+        assert res[i]["gerbicz_checks"] == 1 and res[i]["gerbicz_failures"] == 0
+    b.close()
+
+
+def test_batch_gerbicz_detects_corruption(pg, gmp):
+    """A digit changed by +1 stays inside its range, so only the Gerbicz check
+    can see it: the candidate fails its verification, goes back to its last
+    verified residue and still ends exact; the others are untouched."""
+    cands = _passing(78, 3, 7000, 9000, pg)
+    b = pg.Batch(4)
+    b.set_gerbicz(1000)
+    for i, (k, n) in enumerate(cands):
+        b.submit(k, n, i)
+    b.run(3500)
+    b.debug_corrupt(1, 37, 1)
+    b.run(0)
+    res = {r["tag"]: r for r in b.poll()}
+    assert len(res) == len(cands)
+    assert res[1]["gerbicz_failures"] >= 1 and res[1]["gerbicz_checks"] >= 2
+    for i, (k, n) in enumerate(cands):
+        N = _N(k, n)
+        y = gmp.powmod(res[i]["base"], (N - 1) // 2, N)
+        assert res[i]["status"] == 0
+        assert res[i]["res64"] == y & M64 and res[i]["verdict"] == (y == N - 1), i
+        if i != 1:
+            assert res[i]["gerbicz_failures"] == 0
+    b.close()
+
+
+def test_batch_without_gerbicz_flag(pg, gmp):
+    cands = _passing(79, 3, 3000, 4000, pg)
+    b = pg.Batch(4, flags=pg.FLAG_NO_GERBICZ)
+    for i, (k, n) in enumerate(cands):
+        b.submit(k, n, i)
+    b.run(0)
+    res = {r["tag"]: r for r in b.poll()}
+    for i, (k, n) in enumerate(cands):
+        N = _N(k, n)
+        y = gmp.powmod(res[i]["base"], (N - 1) // 2, N)
+        assert res[i]["res64"] == y & M64 and res[i]["gerbicz_checks"] == 0
+    b.close()
