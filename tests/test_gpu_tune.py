@@ -33,7 +33,8 @@ def test_autotune_one_residue_picks_a_valid_shape(pg):
     assert (got["f0"], got["f1"], got["g_inner"]) == (chosen[0]["f0"], chosen[0]["f1"], chosen[0]["g_inner"])
 
 
-@pytest.mark.parametrize("k,n", [(1000003, 400000), (999999, 1500000)])
+@pytest.mark.parametrize("k,n", [(3, 60000), (999, 250000), (1000003, 400000), (878261, 1048576),
+                                 (999999, 1500000)])
 def test_every_shape_is_exact_against_gmp(pg, gmp, k, n):
     """Each compiled shape at the length of (k, n), set by hand, squares a random
     residue 60 times exactly."""
