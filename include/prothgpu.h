@@ -174,6 +174,9 @@ int pg_prefilter_noalloc(const uint64_t* d_ks, const uint32_t* d_ns, size_t coun
 /* ---- batched engine: many candidates per launch, grouped by FFT length ----
  * Replaces the reference's worker pool (dcore.cpp:84-193 dispatch with
  * worker.cpp:27-69 run_task_with_ctx over PROTH_FF_BATCH k lists). */
+/* max_slots_per_class: at most 13107 (65535 with PG_FLAG_NO_GERBICZ), since each
+ * candidate of a Gerbicz-checked class holds five slots and a launch maps slots
+ * to gridDim.y. */
 int pg_batch_create(uint32_t max_slots_per_class, uint32_t flags, pg_batch** out);
 int pg_batch_destroy(pg_batch* b);
 /* Queue one candidate; the gate and base choice run on the host at submit. */
