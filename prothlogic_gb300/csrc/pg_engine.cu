@@ -62,7 +62,7 @@ struct Shape {
 };
 static std::map<std::pair<int, int>, Shape> g_tuned;  // (lg, mode) -> autotuned shape
 
-static const int kMinLg = 8, kMaxLg = 18;
+static const int kMinLg = 8, kMaxLg = 19;
 static const double kMinBitsPerDigit = 6.0;   // below this the run carries do not settle
 static const double kMaxBitsPerDigit = 24.0;  // balanced digits stay within int32 with room for carries
 
@@ -79,6 +79,7 @@ static bool plan_radices(int lg, int F[MAX_PASSES], int& P) {
         case 16: P = 3; F[0] = 16; F[1] = 64; F[2] = 64; return true;
         case 17: P = 3; F[0] = 32; F[1] = 64; F[2] = 64; return true;
         case 18: P = 3; F[0] = 64; F[1] = 64; F[2] = 64; return true;
+        case 19: P = 3; F[0] = 128; F[1] = 64; F[2] = 64; return true;
         default: return false;
     }
 }
@@ -236,10 +237,10 @@ static void put_weights(unsigned n, unsigned M) {
 
 // Largest bits per digit allowed at each length (roundoff stays well under 0.4).
 // Measured on GB300 (max |err| over 300 squarings of random residues, k = 999999):
-// at 2^8 .. 2^18 the error reaches ~0.05 around 21.5 .. 19 bits per digit; the
+// at 2^8 .. 2^19 the error reaches ~0.05 around 21.5 .. 19 bits per digit; the
 // table stays about half a bit to a bit below that (the 0.4 guard bumps anyway).
 static double max_bits_per_digit(int lg) {
-    static const double t[] = {21.0, 20.5, 20.5, 20.0, 20.0, 19.5, 19.0, 18.5, 18.5, 18.0, 17.5};
+    static const double t[] = {21.0, 20.5, 20.5, 20.0, 20.0, 19.5, 19.0, 18.5, 18.5, 18.0, 17.5, 17.0};
     return t[std::min(std::max(lg - kMinLg, 0), kMaxLg - kMinLg)];
 }
 

@@ -466,3 +466,19 @@ def test_batch_without_gerbicz_flag(pg, gmp):
         y = gmp.powmod(res[i]["base"], (N - 1) // 2, N)
         assert res[i]["res64"] == y & M64 and res[i]["gerbicz_checks"] == 0
     b.close()
+
+
+def test_largest_length_vs_gmp(pg, gmp):
+    """2^19 points, the length of the reference console's largest candidate
+    199971*2^5435752+1: squarings from a random residue equal GMP's."""
+    k, n = 199971, 5435752
+    N = _N(k, n)
+    x = random.Random(19).randrange(N)
+    want = gmp.square_chain(x, 100, N, every=50)
+    with pg.Engine(k, n) as e:
+        assert e.fft_len == 1 << 19
+        e.set_residue(x)
+        for w in want:
+            e.square(50)
+            assert e.get_residue() == w
+        assert e.max_err() < 0.4

@@ -34,7 +34,7 @@ def test_autotune_one_residue_picks_a_valid_shape(pg):
 
 
 @pytest.mark.parametrize("k,n", [(3, 60000), (999, 250000), (1000003, 400000), (878261, 1048576),
-                                 (999999, 1500000)])
+                                 (999999, 1500000), (199971, 5435752)])
 def test_every_shape_is_exact_against_gmp(pg, gmp, k, n):
     """Each compiled shape at the length of (k, n), set by hand, squares a random
     residue 60 times exactly."""

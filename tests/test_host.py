@@ -58,7 +58,7 @@ def test_gate_and_base_match_oracle(oracle, gmp):
 
 def test_fft_length_choice():
     prev = 0
-    for n in [2048, 4096, 8192, 32768, 65536, 131072, 262144, 524288, 1 << 20]:
+    for n in [2048, 4096, 8192, 32768, 65536, 131072, 262144, 524288, 1 << 20, 5435752]:
         L = pg.pick_fft_len(3, n)
         assert L >= prev and L & (L - 1) == 0
         assert n / L <= 19.5
@@ -66,6 +66,8 @@ def test_fft_length_choice():
     assert pg.pick_fft_len(3, 1 << 20) == 65536
     assert pg.pick_fft_len(3, 65536) == 4096
     assert pg.pick_fft_len(3, 100) == 0  # below the smallest supported residue
+    assert pg.pick_fft_len(199971, 5435752) == 1 << 19  # the reference console's largest candidate
+    assert pg.pick_fft_len(3, 9_000_000) == 0  # beyond 17 bits per digit at 2^19
 
 
 def test_workloads_are_seeded():
