@@ -9,9 +9,10 @@ verification of all K blocks runs inside the last timed step.
 
   value  device time (CUDA events on the engine's stream) per squaring, residue
          resident on the device, L2 flushed between steps;
-  e2e    the same metric through the public C ABI with host buffers: every step
-         uploads its input residue (pg_set_residue, H2D), squares 1,000 times
-         and returns a verified result (pg_get_residue, D2H);
+  e2e    the same metric through the public C ABI with host buffers, one
+         step per run of the configuration: upload the input residue
+         (pg_set_residue, H2D), 10,000 squarings with a Gerbicz check every
+         1,000, return the verified result (pg_get_residue, D2H);
   --impl reference  the reference algorithm on this host's cores (the C oracle
          restatement of prothlogic4.2's engine; the reference's AVX-512 code
          itself only builds on x86-64), same metric and config.
@@ -38,6 +39,7 @@ from prothlogic_gb300 import workloads  # noqa: E402
 METRIC = "ns per mod-squaring (n=1,048,576)"
 UNIT = "ns/squaring"
 SQ_PER_STEP = 1000
+E2E_SQ_PER_STEP = 10 * SQ_PER_STEP  # one run of the configuration: 10,000 squarings, Gerbicz every 1,000
 
 
 def measured_peaks():
@@ -124,16 +126,20 @@ def dp_ops_per_point(plan_F):
 
 
 def profile_traffic():
-    """DRAM bytes of one squaring (its 5 kernels) from the committed ncu launch-list summary, or None."""
+    """(DRAM bytes of one squaring, the launch shape they were captured on) from
+    the committed ncu launch-list summary, or (None, None)."""
     path = os.path.join(ROOT, "profiles", "squaring_n1048576.md")
+    got, shape = None, None
     try:
         with open(path) as f:
             for ln in f:
                 if ln.startswith("dram_bytes_per_squaring:"):
-                    return float(ln.split(":", 1)[1])
+                    got = float(ln.split(":", 1)[1])
+                elif ln.startswith("profiled_shape:"):
+                    shape = ln.split(":", 1)[1].strip()
     except OSError:
         pass
-    return None
+    return got, shape
 
 
 def dist_setup():
@@ -223,7 +229,9 @@ def _chosen(rows):
     """'f0xf1[xf2] g_mid/g_inner (of N shapes)' for the shape the autotuner picked."""
     r = [x for x in rows if x["chosen"]][0]
     radices = "x".join(str(r[f]) for f in ("f0", "f1", "f2")[: r["passes"]])
-    return (f"{radices} g{r['g_mid']}/{r['g_inner']} {r['tpb']} thread(s)/butterfly "
+    mid = (f"middle fused in clusters of {r['cluster']} CTAs" if r.get("cluster")
+           else f"g{r['g_mid']}/{r['g_inner']}")
+    return (f"{radices} {mid} {r['tpb']} thread(s)/butterfly "
             f"(fastest of {len(rows)} bit-identical shapes)")
 
 
@@ -395,8 +403,13 @@ def run_gpu(args, world, rank, local, pgd):
     # events around each (untimed; serialised like the ncu launch list, so the
     # shares compare with profiles/squaring_n1048576.md)
     prof = [eng.profile_step() for _ in range(20)]
-    names = ["k_first", "k_mid_fwd", "k_inner", "k_mid_inv", "k_last"] if len(prof[0]) == 5 else \
-        ["k_first", "k_inner", "k_last"]
+    chosen = [r for r in tune_rows if r["chosen"]][0]
+    if len(prof[0]) == 5:
+        names = ["k_first", "k_mid_fwd", "k_inner", "k_mid_inv", "k_last"]
+    elif chosen["passes"] == 3:
+        names = ["k_first", "k_block", "k_last"]  # middle passes fused in one cluster kernel
+    else:
+        names = ["k_first", "k_inner", "k_last"]
     per_k = [statistics.median(p[i] for p in prof) * 1e3 for i in range(len(names))]
     kernels_live = [{"kernel": nm, "us": t, "share": t / sum(per_k)} for nm, t in zip(names, per_k)]
     value = total_ms * 1e6 / (K * SQ_PER_STEP * world)
@@ -412,17 +425,19 @@ def run_gpu(args, world, rank, local, pgd):
     except (OSError, KeyError, IndexError):
         pass
 
-    # e2e through the public API with host buffers, one verified block per step
+    # e2e through the public API with host buffers: each step is one run of the
+    # configuration (set the residue, 10,000 squarings with a Gerbicz check every
+    # 1,000, read back the verified residue)
     eng.set_gerbicz(SQ_PER_STEP, 0)
     x = a
     barrier(pgd)
     t0 = time.perf_counter()
     for _ in range(K):
         eng.set_residue(x)
-        eng.square(SQ_PER_STEP)
+        eng.square(E2E_SQ_PER_STEP)
         x = eng.get_residue()
     e2e_s = max_over_ranks(pgd, time.perf_counter() - t0)
-    e2e = e2e_s * 1e9 / (K * SQ_PER_STEP * world)
+    e2e = e2e_s * 1e9 / (K * E2E_SQ_PER_STEP * world)
     nl_in = (x.bit_length() + 63) // 64
     h2d = M * 4 + (M // 8) * 16 + 112          # digits, run carries, slot state
     d2h = M * 4 + 8 + 112                       # canonical digits, top digit, slot state
@@ -437,7 +452,7 @@ def run_gpu(args, world, rank, local, pgd):
     dp_ops = dp_ops_per_point(_chosen_radices(tune_rows)) * M
     dp_rate = dp_ops / t_sq / 1e12                 # T instr/s
     dp_peak = fp64_tflops / 2.0                    # DFMA instr/s from the live probe
-    traffic = profile_traffic()
+    traffic, traffic_shape = profile_traffic()
 
     if rank != 0:
         eng.close()
@@ -459,9 +474,9 @@ def run_gpu(args, world, rank, local, pgd):
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved_gbs / hbm_peak if hbm_peak else None, "traffic": traffic,
                      "kernels_live": kernels_live,
-                     "note": "measured hbm_gbs peak; unit = one squaring (its 5 kernels); traffic = DRAM "
-                             "bytes of those 5 launches under ncu (cold caches; L2-resident in steady "
-                             "state); the real bound is the FP64 pipe, see roofline_fp64"},
+                     "note": f"measured hbm_gbs peak; unit = one squaring (its {len(names)} kernels); traffic "
+                             f"= DRAM bytes of one squaring's launches under ncu (shape {traffic_shape}; cold caches; "
+                             "L2-resident in steady state); the real bound is the FP64 pipe, see roofline_fp64"},
         "roofline_fp64": {"bound": "fp64", "achieved": dp_rate, "peak": dp_peak, "unit": "T DP instr/s",
                           "frac": dp_rate / dp_peak, "dp_instr_per_squaring": dp_ops,
                           "peak_source": "live DFMA probe (pg_measure_fp64_peak), of measured",
@@ -471,7 +486,8 @@ def run_gpu(args, world, rank, local, pgd):
         "cpu_baseline": {"value": cpu_ns, "unit": UNIT, "cores": 1, "kind": cpu_kind,
                          "sample": f"{cpu_used} squarings at n=1048576, L={cpu_L}, one host thread"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "note": "set_residue + 1,000 squarings + verified get_residue per step"},
+                "note": "per step: set_residue (H2D) + 10,000 squarings with a Gerbicz check every 1,000 + "
+                        "verified get_residue (D2H)"},
         "clocks": clocks,
         "gpu_launches": launches,
         "batched": batched,

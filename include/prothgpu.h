@@ -219,6 +219,8 @@ int pg_batch_set_gerbicz(pg_batch* b, uint64_t block);
 typedef struct pg_tune_result {
     uint32_t lg, slots, passes, f0, f1, f2, g_mid, g_inner;
     uint32_t tpb;       /* threads per radix-4 butterfly: 1, or 2 (paired lanes, shorter FP64 chains) */
+    uint32_t cluster;   /* one residue, three-pass plans: CTAs of the cluster that runs the middle passes
+                           as one kernel (0: three kernels) */
     double us_per_step; /* one squaring of every slot */
     int32_t valid;      /* residues equal to the other shapes', no roundoff or range flag */
     int32_t chosen;

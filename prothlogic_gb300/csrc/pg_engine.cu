@@ -59,6 +59,7 @@ struct Shape {
     int F[MAX_PASSES] = {0, 0, 0};
     int gm = 0, gi = 0;
     int tpb = 1;  // threads per radix-4 butterfly in every kernel of the step
+    int cl = 0;   // one residue: middle passes fused into one cluster kernel of cl CTAs per block (0: three kernels)
 };
 static std::map<std::pair<int, int>, Shape> g_tuned;  // (lg, mode) -> autotuned shape
 
@@ -279,6 +280,7 @@ struct Pool {
     bool big = false;
     int gm[2] = {2, 2}, gi[2] = {2, 2};  // middle / inner columns per CTA: [0] one residue per launch, [1] many
     int tpb[2] = {1, 1};                 // threads per radix-4 butterfly (2: paired lanes)
+    int cl = 0;                          // solo steps: cluster CTAs of the fused middle (k_block), 0: off
     bool capturing = false;
     GridBar* bar = nullptr;      // grid barrier of the persistent kernel
     int persist_grid = 0;        // co-resident CTAs for it (0: not available)
@@ -328,10 +330,56 @@ static void launch_last(int tpb, dim3 g, cudaStream_t s, const Slot* sl, int bas
     else launch_pdl(k_last<F0, 1>, g, dim3(2 * F0), s, sl, base, pd, one);
 }
 
+// The fused middle of a three-pass step: one cluster of CL CTAs per block of
+// F*F points (F = F[1] = F[2]), F*(F/CL)/4*TPB threads per CTA.
+typedef void (*BlockFn)(const PlanDev, const Slot);
+static BlockFn block_fn(int F, int CL, int tpb) {
+#define PG_BLOCK(FF, CC, TT) \
+    if (F == FF && CL == CC && tpb == TT) return k_block<FF, CC, TT>;
+    PG_BLOCK(64, 4, 1) PG_BLOCK(64, 8, 1) PG_BLOCK(64, 16, 1) PG_BLOCK(64, 4, 2) PG_BLOCK(64, 8, 2)
+    PG_BLOCK(64, 16, 2) PG_BLOCK(32, 4, 1) PG_BLOCK(32, 8, 1) PG_BLOCK(32, 4, 2) PG_BLOCK(32, 8, 2)
+#undef PG_BLOCK
+    return nullptr;
+}
+static bool block_instance(int F, int CL, int tpb) { return block_fn(F, CL, tpb) != nullptr; }
+
+// Whether the current device can hold a cluster of this instance (clusters
+// above 8 CTAs are outside the portable size and need the kernel's opt-in
+// attribute, set here).  Cached per (device, instance).
+static bool block_fits(int F, int CL, int tpb) {
+    BlockFn fn = block_fn(F, CL, tpb);
+    if (!fn) return false;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    static std::mutex mu;
+    static std::map<std::pair<int, BlockFn>, bool> memo;
+    std::lock_guard<std::mutex> lk(mu);
+    const auto key = std::make_pair(dev, fn);
+    auto it = memo.find(key);
+    if (it != memo.end()) return it->second;
+    if (CL > 8) cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(CL);
+    cfg.blockDim = dim3(F * (F / CL) / 4 * tpb);
+    int clusters = 0;
+    const bool ok = cudaOccupancyMaxActiveClusters(&clusters, (const void*)fn, &cfg) == cudaSuccess && clusters > 0;
+    cudaGetLastError();  // a refused size is an answer, not an error to keep
+    memo[key] = ok;
+    return ok;
+}
+
+// Kernels per step: first pass, the middle (three kernels, or one fused
+// cluster kernel for a solo step of a pool with cl set), last pass.
+static int step_parts(const Pool* p, bool solo) {
+    const PlanDev& d = p->plan->dev;
+    if (d.P != 3) return 3;
+    return (solo && p->cl > 0 && d.F[1] == d.F[2] && block_instance(d.F[1], p->cl, p->tpb[0])) ? 3 : 5;
+}
+
 static int enqueue_step_part(Pool* p, int part, int base, int count, bool solo = false);
 
 static int enqueue_step(Pool* p, int base, int count, bool solo = false) {
-    const int parts = p->plan->dev.P == 3 ? 5 : 3;
+    const int parts = step_parts(p, solo);
     for (int i = 0; i < parts; ++i) {
         const int rc = enqueue_step_part(p, i, base, count, solo);
         if (rc) return rc;
@@ -344,9 +392,10 @@ static int enqueue_step(Pool* p, int base, int count, bool solo = false) {
 // solo: one residue squared for exactly the steps the host runs (descriptor by value).
 static int enqueue_step_part(Pool* p, int part, int base, int count, bool solo) {
     const PlanDev& d = p->plan->dev;
-    const int parts = d.P == 3 ? 5 : 3;
-    if (part < 0 || part >= parts || base < 0 || count < 1 || base + count > p->S) return PG_EINVAL;
     if (solo && count != 1) return PG_EINVAL;
+    const int parts = step_parts(p, solo);
+    if (part < 0 || part >= parts || base < 0 || count < 1 || base + count > p->S) return PG_EINVAL;
+    const bool fused = d.P == 3 && parts == 3;
     Slot one;
     memset(&one, 0, sizeof(one));
     if (solo) one = p->hslots[base];
@@ -371,6 +420,9 @@ static int enqueue_step_part(Pool* p, int part, int base, int count, bool solo) 
             case 64: launch_last<64>(T, g0, p->stream, p->dslots, base, d, one); break;
             case 128: launch_last<128>(T, g0, p->stream, p->dslots, base, d, one); break;
         }
+    } else if (fused) {
+        const BlockFn fn = block_fn(d.F[1], p->cl, T);
+        if (fn && ++nl) launch_pdl(fn, dim3(d.F[0] * p->cl), dim3(d.F[1] * (d.F[1] / p->cl) / 4 * T), p->stream, d, one);
     } else if ((d.P == 3 && part == 2) || (d.P == 2 && part == 1)) {
         const dim3 gi(d.M / (Fl * Gi), count);
 #define PG_INNER2(FF, GG, LP, TT) \
@@ -455,6 +507,7 @@ static int pool_create(int lg, int S, Pool** out, int mode = 0, const Shape* sha
         p->gm[0] = p->gm[1] = sh.gm;
         p->gi[0] = p->gi[1] = sh.gi;
         p->tpb[0] = p->tpb[1] = sh.tpb;
+        p->cl = sh.cl;
     } else {
         std::lock_guard<std::mutex> lk(g_cache_mu);
         for (int m = 0; m < 2; ++m) {
@@ -466,9 +519,12 @@ static int pool_create(int lg, int S, Pool** out, int mode = 0, const Shape* sha
                 p->gm[m] = t.gm;
                 p->gi[m] = t.gi;
                 p->tpb[m] = t.tpb;
+                if (m == 0) p->cl = t.cl;
             }
         }
     }
+    if (p->cl && !(plan->dev.P == 3 && plan->dev.F[1] == plan->dev.F[2] && block_fits(plan->dev.F[1], p->cl, p->tpb[0])))
+        p->cl = 0;  // no such cluster on this device: three middle kernels
     p->hslots.resize(S);
     p->slot_n.assign(S, 0);
     const size_t M = p->M, nruns = M / RUN;
@@ -659,7 +715,7 @@ static int pool_run(Pool* p, long long steps, bool use_graph, int base = 0, int 
     while (steps > 0) {
         if (ge && steps >= GSTEPS) {
             PG_CK(cudaGraphLaunch(ge, p->stream));
-            g_launches += (unsigned long long)GSTEPS * (p->plan->dev.P == 3 ? 5 : 3);
+            g_launches += (unsigned long long)GSTEPS * step_parts(p, solo);
             steps -= GSTEPS;
         } else {
             int rc = enqueue_step(p, base, count, solo);
@@ -714,7 +770,7 @@ static int pool_run_pair(Pool* p, long long steps, int a) {
     PG_CK(cudaEventRecord(fork, p->stream));
     PG_CK(cudaStreamWaitEvent(p->stream2, fork, 0));
     int rc = PG_OK;
-    const int parts = p->plan->dev.P == 3 ? 5 : 3;
+    const int parts = step_parts(p, true);
     while (steps > 0 && rc == PG_OK) {
         if (ga && steps >= GSTEPS) {
             if (cudaGraphLaunch(ga, p->stream) != cudaSuccess || cudaGraphLaunch(gb, p->stream2) != cudaSuccess)
@@ -1429,7 +1485,7 @@ int pg_time_squarings(pg_engine* e, uint64_t iters, double* ms, uint32_t* kernel
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     *ms = f;
-    if (kernels_per_step) *kernels_per_step = e->pool->plan->dev.P == 3 ? 5 : 3;
+    if (kernels_per_step) *kernels_per_step = (uint32_t)step_parts(e->pool, true);
     e->armed = false;  // squarings outside the Gerbicz bookkeeping
     if (!rc) e->squarings += iters;
     return rc;
@@ -1446,7 +1502,7 @@ int pg_profile_step(pg_engine* e, double* times, uint32_t cap, uint32_t* count) 
     st.partner = SX;
     rc = slot_write(e, SX, st);
     if (rc) return rc;
-    const int parts = e->pool->plan->dev.P == 3 ? 5 : 3;
+    const int parts = step_parts(e->pool, true);
     std::vector<cudaEvent_t> ev(parts + 1);
     for (auto& x : ev) PG_CK(cudaEventCreate(&x));
     PG_CK(cudaEventRecord(ev[0], e->pool->stream));

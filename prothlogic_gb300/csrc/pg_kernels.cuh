@@ -18,6 +18,8 @@
 //   k_inner   last pass forward, pointwise square, last pass inverse
 //   k_last    pass 0 inverse, fused with unweight, rounding + max |err|,
 //             the Montgomery fold and the in-run carry
+//   k_block   one residue, P == 3: the three middle kernels in one, a
+//             thread-block cluster per block of the spectrum
 // All arithmetic on the transform is FP64; rounding, fold and carries are
 // exact integer (int64 / int128) work.  Slots (candidates) run side by side:
 // blockIdx.y is the slot.
@@ -825,6 +827,126 @@ __global__ void __launch_bounds__(2 * F0 * TPB) k_last(const Slot* __restrict__ 
         // the partner index is fixed by the host before the step: safe to read early
         tile_last<F0, 2 * F0 * TPB>(sl, slots[st->partner], pl, blockIdx.x, threadIdx.x, tile, cl, ch, BlockSync(),
                                     PdlActive{st, true});
+    }
+    pdl_trigger();
+}
+
+// ---------------------------------------------------------------------------
+// The middle of a three-pass squaring in ONE kernel, on a thread-block cluster.
+//
+// After pass 0 the spectrum splits into F0 independent contiguous blocks of
+// Mi[1] = F * F points (F = F[1] = F[2]); pass 1 forward, pass 2 forward, the
+// square, pass 2 inverse and pass 1 inverse never look outside a block.  A
+// cluster of CL CTAs owns one block: each CTA does the pass-1 transforms of
+// G = F / CL columns, hands every value to the CTA that owns its pass-2 group
+// by a store into that CTA's shared memory (distributed shared memory), squares
+// G groups of F contiguous points, hands them back the same way, and finishes
+// the inverse pass-1 transforms of its columns.  The two hand-overs replace two
+// kernel boundaries (and their L2 round trips) by cluster barriers.  The
+// operations on every value and their order are those of k_mid_fwd, k_inner and
+// k_mid_inv, so the residues are bit-identical to the three-kernel sequence.
+// Single residue only (the descriptor by value, as `one` above).
+
+__device__ __forceinline__ unsigned cluster_ctarank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// Address of the same shared variable in CTA `rank` of this cluster.
+__device__ __forceinline__ unsigned mapa_shared(unsigned local, unsigned rank) {
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void st_cluster(unsigned addr, double2 v) {
+    asm volatile("st.shared::cluster.v2.f64 [%0], {%1, %2};" ::"r"(addr), "d"(v.x), "d"(v.y) : "memory");
+}
+// Cluster barrier halves.  Every thread of every CTA of the cluster executes
+// each of them the same number of times (no early exit in k_block).
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+    asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+template <int F, int CL, int TPB>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(F * (F / CL) / 4 * TPB)
+    k_block(const PlanDev pl, const Slot one) {
+    constexpr int G = F / CL;                // pass-1 columns = pass-2 groups per CTA
+    constexpr int NT = F * G / 4 * TPB;
+    constexpr int PER = F * G / NT;
+    static_assert(G >= 2 && F * G % NT == 0, "block shape");
+    __shared__ __align__(16) double2 ta[F * G];  // pass-1 tile: element (row q, column t) at q * G + t
+    __shared__ __align__(16) double2 tb[F * G];  // pass-2 tile: element (group g, point i) at g * F + i
+    const int tid = threadIdx.x;
+    const unsigned c = cluster_ctarank();
+    const int blk = blockIdx.x / CL;
+    const int S = pl.S[1];                   // == F
+    double2* bp = one.spec + (size_t)blk * pl.Mi[1];
+    const int r0 = (int)c * G;
+    const double2* __restrict__ tw = pl.tw[1];
+    double2 ct[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        ct[i] = tw[(e / G) * S + r0 + e % G];
+    }
+    cluster_arrive_relaxed();  // paired with the wait before the first remote store
+    pdl_wait();
+    if (blockIdx.x == 0 && tid == 0) one.st->step += 1;  // nobody reads step until k_last
+    // pass 1 forward on columns r0 .. r0+G-1
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        ta[e] = bp[r0 + e % G + (e / G) * S];
+    }
+    __syncthreads();
+    smem_fft_fwd<F, G, NT, false>(ta, pl.wF[1], tid, BlockSync());
+    cluster_wait();  // every CTA of the cluster is running
+    // value (row q, column r0+t) is point r0+t of group q: CTA q / G, slot (q % G) * F + r0 + t
+    const unsigned tb_local = smem_u32(tb);
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        const int q = e / G, t = e % G;
+        const unsigned dst = tb_local + (unsigned)(((q % G) * F + r0 + t) * (int)sizeof(double2));
+        st_cluster(mapa_shared(dst, (unsigned)(q / G)), cmul(ta[e], ct[i]));
+    }
+    cluster_arrive();
+    cluster_wait();
+    // pass 2 on groups c*G .. c*G+G-1: forward, square, inverse
+    smem_fft_fwd<F, G, NT, true>(tb, pl.wF[2], tid, BlockSync());
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        const double2 z = tb[e];
+        tb[e] = make_double2(fma(z.x, z.x, -(z.y * z.y)), (z.x + z.x) * z.y);
+    }
+    __syncthreads();
+    smem_fft_inv<F, G, NT, true>(tb, pl.wF[2], tid, BlockSync());
+    // point i of group c*G+g is (row c*G+g, column i): CTA i / G, slot (c*G+g) * G + i % G
+    const unsigned ta_local = smem_u32(ta);
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        const int g = e / F, pt = e % F;
+        const unsigned dst = ta_local + (unsigned)((((int)c * G + g) * G + pt % G) * (int)sizeof(double2));
+        st_cluster(mapa_shared(dst, (unsigned)(pt / G)), tb[e]);
+    }
+    cluster_arrive();
+    cluster_wait();  // after this no CTA touches another's shared memory
+    // pass 1 inverse on columns r0 .. r0+G-1
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        ta[e] = cmulc(ta[e], ct[i]);
+    }
+    __syncthreads();
+    smem_fft_inv<F, G, NT, false>(ta, pl.wF[1], tid, BlockSync());
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        bp[r0 + e % G + (e / G) * S] = ta[e];
     }
     pdl_trigger();
 }

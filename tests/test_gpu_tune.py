@@ -67,6 +67,29 @@ def test_tuned_engine_matches_large_configuration(pg):
     pg.tune_clear()
 
 
+@pytest.mark.parametrize("cluster,tpb", [(4, 1), (8, 1), (16, 1), (8, 2), (16, 2)])
+def test_fused_middle_exact_with_gerbicz(pg, cluster, tpb):
+    """n = 2^20 with the three middle passes of each squaring in one cluster
+    kernel (shape set by hand) and the Gerbicz check on, whose products still run
+    the three-kernel middle: RES64 after 1,000 and 2,000 squarings equal the GMP
+    values, and a squaring is three kernels."""
+    with open(GOLDEN) as f:
+        g = json.load(f)["large"]
+    pg.tune_set(pg.TUNE_ONE, {"lg": 16, "slots": 1, "passes": 3, "f0": 16, "f1": 64, "f2": 64,
+                              "g_mid": 2, "g_inner": 2, "tpb": tpb, "cluster": cluster})
+    try:
+        with pg.Engine(g["k"], g["n"]) as e:
+            e.set_residue(g["a"])
+            for i in range(2):
+                e.square(g["every"])
+                assert format(e.get_residue() & M64, "016x") == g["res64"][i], i
+            assert e.stats()["gerbicz_checks"] >= 2
+            _, kernels = e.time_squarings(50)
+            assert kernels == 3
+    finally:
+        pg.tune_clear()
+
+
 def test_tuned_batch_full_tests_exact(pg, gmp):
     rows = pg.autotune(12, slots=64, iters=50)
     assert any(r["chosen"] for r in rows) and all(r["valid"] for r in rows)
