@@ -534,10 +534,27 @@ def ncu_batch_target():
     return 0
 
 
-def ncu_target():
-    """Small profiling target: one n = 1,048,576 residue, 200 squarings, no Gerbicz."""
+def parse_shape(spec, lg):
+    """'64x32x32,gm=2,gi=4,tpb=1,cl=8' -> a tune-result dict for 2^lg points."""
+    parts = spec.split(",")
+    radices = [int(x) for x in parts[0].split("x")]
+    shape = {"lg": lg, "slots": 1, "passes": len(radices), "f0": radices[0], "f1": radices[1],
+             "f2": radices[2] if len(radices) > 2 else 0, "g_mid": 2, "g_inner": 2, "tpb": 1, "cluster": 0}
+    names = {"gm": "g_mid", "gi": "g_inner", "tpb": "tpb", "cl": "cluster"}
+    for kv in parts[1:]:
+        key, val = kv.split("=")
+        shape[names[key]] = int(val)
+    return shape
+
+
+def ncu_target(shape=None):
+    """Small profiling target: one n = 1,048,576 residue, 200 squarings, no
+    Gerbicz; `shape` (see parse_shape) pins the launch shape."""
     import prothlogic_gb300 as pg
     k, n = workloads.large()
+    if shape:
+        lg = pg.pick_fft_len(k, n).bit_length() - 1
+        pg.tune_set(pg.TUNE_ONE, parse_shape(shape, lg))
     e = pg.Engine(k, n, flags=pg.FLAG_NO_GERBICZ)
     e.set_residue(5)
     e.square(200)
@@ -553,11 +570,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ncu-target", action="store_true", help="run only the small profiling target")
+    ap.add_argument("--shape", default=None, help="launch shape of the profiling target, e.g. 64x32x32,gi=4,cl=8")
     ap.add_argument("--uneven-full", action="store_true", help="run the whole uneven batch to completion")
     ap.add_argument("--ncu-batch-target", action="store_true", help="run only the small batched profiling target")
     args = ap.parse_args()
     if args.ncu_target:
-        return ncu_target()
+        return ncu_target(args.shape)
     if args.ncu_batch_target:
         return ncu_batch_target()
     if args.uneven_full:
