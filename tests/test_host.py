@@ -88,3 +88,48 @@ def test_engine_fails_loudly_without_device():
         pytest.skip("a GPU is present")
     with pytest.raises(pg.ProthGpuError):
         pg.Engine(3, 4096)
+
+
+@pytest.mark.parametrize("cname,pystruct", [("pg_result", pg.PgResult), ("pg_tune_result", pg.PgTuneResult)])
+def test_abi_struct_layout_matches_binding(tmp_path, cname, pystruct):
+    """The ctypes mirrors have the C header's size and field offsets (compiled
+    with the host C compiler against include/prothgpu.h)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = [f for f, _ in pystruct._fields_]
+    src = tmp_path / "layout.c"
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "prothgpu.h"', "int main(void) {",
+             f'    printf("%zu\\n", sizeof({cname}));']
+    lines += [f'    printf("%zu\\n", offsetof({cname}, {f}));' for f in fields]
+    lines += ["    return 0;", "}"]
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.check_call([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = [int(x) for x in subprocess.check_output([str(exe)]).split()]
+    assert got[0] == __import__("ctypes").sizeof(pystruct)
+    for f, off in zip(fields, got[1:]):
+        assert getattr(pystruct, f).offset == off, f
+
+
+def test_tune_set_validates_cluster_shapes():
+    """Fused-middle shapes are accepted only where a cluster kernel is compiled:
+    three passes with equal middle and inner radices (host logic, no device)."""
+    base = {"lg": 16, "slots": 1, "passes": 3, "f0": 64, "f1": 32, "f2": 32, "g_mid": 2, "g_inner": 4, "tpb": 1}
+    try:
+        for cl in (0, 4, 8):
+            pg.tune_set(pg.TUNE_ONE, dict(base, cluster=cl))
+            assert pg.tune_get(16, pg.TUNE_ONE)["cluster"] == cl
+        pg.tune_set(pg.TUNE_ONE, dict(base, f0=16, f1=64, f2=64, g_inner=2, cluster=16))
+        for bad in (dict(base, cluster=16),                      # no 32-point cluster of 16 CTAs
+                    dict(base, cluster=3),
+                    dict(base, f0=16, f1=64, f2=64, g_inner=2, cluster=2),     # no cluster of 2
+                    dict(base, f0=32, f1=32, f2=64, g_inner=2, cluster=8),    # middle and inner radices differ
+                    {"lg": 12, "slots": 1, "passes": 2, "f0": 64, "f1": 64, "f2": 0, "g_mid": 2, "g_inner": 2,
+                     "tpb": 1, "cluster": 8}):                  # two-pass plans have no middle
+            with pytest.raises(pg.ProthGpuError):
+                pg.tune_set(pg.TUNE_ONE, bad)
+    finally:
+        pg.tune_clear()
