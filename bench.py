@@ -231,8 +231,10 @@ def _chosen(rows):
     radices = "x".join(str(r[f]) for f in ("f0", "f1", "f2")[: r["passes"]])
     mid = (f"middle fused in clusters of {r['cluster']} CTAs" if r.get("cluster")
            else f"g{r['g_mid']}/{r['g_inner']}")
-    return (f"{radices} {mid} {r['tpb']} thread(s)/butterfly "
-            f"(fastest of {len(rows)} bit-identical shapes)")
+    outer = r.get("tpb_outer") or r["tpb"]
+    tpb = (f"{r['tpb']} thread(s)/butterfly" if outer == r["tpb"]
+           else f"{r['tpb']} thread(s)/butterfly ({outer} in the first and last passes)")
+    return f"{radices} {mid} {tpb} (fastest of {len(rows)} bit-identical shapes)"
 
 
 def _chosen_radices(rows):

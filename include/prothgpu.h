@@ -221,6 +221,7 @@ typedef struct pg_tune_result {
     uint32_t tpb;       /* threads per radix-4 butterfly: 1, or 2 (paired lanes, shorter FP64 chains) */
     uint32_t cluster;   /* one residue, three-pass plans: CTAs of the cluster that runs the middle passes
                            as one kernel (0: three kernels) */
+    uint32_t tpb_outer; /* threads per radix-4 butterfly of the first and last passes (0: tpb) */
     double us_per_step; /* one squaring of every slot */
     int32_t valid;      /* residues equal to the other shapes', no roundoff or range flag */
     int32_t chosen;

@@ -47,7 +47,8 @@ class PgResult(ctypes.Structure):
 
 class PgTuneResult(ctypes.Structure):
     _fields_ = [("lg", _u32), ("slots", _u32), ("passes", _u32), ("f0", _u32), ("f1", _u32), ("f2", _u32),
-                ("g_mid", _u32), ("g_inner", _u32), ("tpb", _u32), ("cluster", _u32), ("us_per_step", ctypes.c_double),
+                ("g_mid", _u32), ("g_inner", _u32), ("tpb", _u32), ("cluster", _u32), ("tpb_outer", _u32),
+                ("us_per_step", ctypes.c_double),
                 ("valid", _i32), ("chosen", _i32)]
 
     def as_dict(self):

@@ -58,7 +58,8 @@ struct Shape {
     int P = 0;
     int F[MAX_PASSES] = {0, 0, 0};
     int gm = 0, gi = 0;
-    int tpb = 1;  // threads per radix-4 butterfly in every kernel of the step
+    int tpb = 1;  // threads per radix-4 butterfly in every kernel of the step ...
+    int tpb0 = 0; // ... except the first and last passes when set (one residue per launch)
     int cl = 0;   // one residue: middle passes fused into one cluster kernel of cl CTAs per block (0: three kernels)
 };
 static std::map<std::pair<int, int>, Shape> g_tuned;  // (lg, mode) -> autotuned shape
@@ -280,6 +281,7 @@ struct Pool {
     bool big = false;
     int gm[2] = {2, 2}, gi[2] = {2, 2};  // middle / inner columns per CTA: [0] one residue per launch, [1] many
     int tpb[2] = {1, 1};                 // threads per radix-4 butterfly (2: paired lanes)
+    int tpb0[2] = {1, 1};                // the same for the first and last passes
     int cl = 0;                          // solo steps: cluster CTAs of the fused middle (k_block), 0: off
     bool capturing = false;
     GridBar* bar = nullptr;      // grid barrier of the persistent kernel
@@ -404,21 +406,22 @@ static int enqueue_step_part(Pool* p, int part, int base, int count, bool solo) 
     const int Gm = p->gm[mode];
     const int Gi = p->gi[mode];
     const int T = p->tpb[mode];
+    const int T0 = p->tpb0[mode];
     const int Fl = d.F[d.P - 1];
     int nl = 0;
     if (part == 0) {
         switch (d.F[0]) {
-            case 16: launch_first<16>(T, g0, p->stream, p->dslots, base, d, one); break;
-            case 32: launch_first<32>(T, g0, p->stream, p->dslots, base, d, one); break;
-            case 64: launch_first<64>(T, g0, p->stream, p->dslots, base, d, one); break;
-            case 128: launch_first<128>(T, g0, p->stream, p->dslots, base, d, one); break;
+            case 16: launch_first<16>(T0, g0, p->stream, p->dslots, base, d, one); break;
+            case 32: launch_first<32>(T0, g0, p->stream, p->dslots, base, d, one); break;
+            case 64: launch_first<64>(T0, g0, p->stream, p->dslots, base, d, one); break;
+            case 128: launch_first<128>(T0, g0, p->stream, p->dslots, base, d, one); break;
         }
     } else if (part == parts - 1) {
         switch (d.F[0]) {
-            case 16: launch_last<16>(T, g0, p->stream, p->dslots, base, d, one); break;
-            case 32: launch_last<32>(T, g0, p->stream, p->dslots, base, d, one); break;
-            case 64: launch_last<64>(T, g0, p->stream, p->dslots, base, d, one); break;
-            case 128: launch_last<128>(T, g0, p->stream, p->dslots, base, d, one); break;
+            case 16: launch_last<16>(T0, g0, p->stream, p->dslots, base, d, one); break;
+            case 32: launch_last<32>(T0, g0, p->stream, p->dslots, base, d, one); break;
+            case 64: launch_last<64>(T0, g0, p->stream, p->dslots, base, d, one); break;
+            case 128: launch_last<128>(T0, g0, p->stream, p->dslots, base, d, one); break;
         }
     } else if (fused) {
         const BlockFn fn = block_fn(d.F[1], p->cl, T);
@@ -507,6 +510,7 @@ static int pool_create(int lg, int S, Pool** out, int mode = 0, const Shape* sha
         p->gm[0] = p->gm[1] = sh.gm;
         p->gi[0] = p->gi[1] = sh.gi;
         p->tpb[0] = p->tpb[1] = sh.tpb;
+        p->tpb0[0] = p->tpb0[1] = sh.tpb0 ? sh.tpb0 : sh.tpb;
         p->cl = sh.cl;
     } else {
         std::lock_guard<std::mutex> lk(g_cache_mu);
@@ -519,6 +523,7 @@ static int pool_create(int lg, int S, Pool** out, int mode = 0, const Shape* sha
                 p->gm[m] = t.gm;
                 p->gi[m] = t.gi;
                 p->tpb[m] = t.tpb;
+                p->tpb0[m] = t.tpb0 ? t.tpb0 : t.tpb;
                 if (m == 0) p->cl = t.cl;
             }
         }

@@ -133,3 +133,17 @@ def test_tune_set_validates_cluster_shapes():
                 pg.tune_set(pg.TUNE_ONE, bad)
     finally:
         pg.tune_clear()
+
+
+def test_bench_module_helpers():
+    """bench.py imports without a GPU; its shape parser and shape label agree."""
+    import importlib
+    import sys
+    sys.path.insert(0, ROOT)
+    bench = importlib.import_module("bench")
+    shape = bench.parse_shape("64x32x32,gm=2,gi=4,tpb=1,cl=8", 16)
+    assert (shape["f0"], shape["f1"], shape["f2"], shape["g_inner"], shape["cluster"]) == (64, 32, 32, 4, 8)
+    row = dict(shape, chosen=1, tpb_outer=2)
+    label = bench._chosen([row, dict(row, chosen=0)])
+    assert label.startswith("64x32x32 middle fused in clusters of 8 CTAs") and "fastest of 2" in label
+    assert bench.dp_ops_per_point((16, 64, 64)) == 126
