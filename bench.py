@@ -17,6 +17,12 @@ verification of all K blocks runs inside the last timed step.
          restatement of prothlogic4.2's engine; the reference's AVX-512 code
          itself only builds on x86-64), same metric and config.
 
+Beside the headline, the line carries the other single-GPU configurations:
+`batched` (4,096 candidates at n = 65,536), `batched_uneven` (2,048 candidates,
+n log-uniform in [8,192, 262,144]) and `single_test` (whole tests at n = 32,768),
+each against one-at-a-time on the GPU and the reference algorithm on all host
+cores.  The serving sweep (Poisson arrivals) runs as prothlogic_gb300/serve.py.
+
 Multi-GPU: candidates do not shard, so N > 1 runs N independent replicas
 (one process per GPU) and `value` is the whole-job time per squaring.
 """
@@ -264,6 +270,47 @@ def cpu_tests_per_hour(cands, sq_sample, budget_s=None):
                       f"({wall:.1f} s), scaled by {scale:.0f} to full tests"}
 
 
+def single_sample(pg, reps=3, cpu_sq=1000):
+    """Configuration 1: whole Proth tests at n = 32768, one at a time on the GPU
+    (pg_proth_test: gate, base, a^k, n - 1 squarings with the Gerbicz check,
+    verdict), next to the reference algorithm's tests/hour on all host cores.
+    The candidate is the first seed-1 draw that passes the reference's
+    small-prime gate (a gated candidate is answered without a squaring)."""
+    cands = workloads.single(16)
+    k, n = next(c for c in cands if not pg.gate_rejects(*c))
+    lg = pg.pick_fft_len(k, n).bit_length() - 1
+    rows = pg.autotune(lg, slots=1, iters=200)
+    r = pg.proth_test(k, n)  # warm-up: plan, weights, graphs
+    secs = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        r = pg.proth_test(k, n)
+        secs.append(time.perf_counter() - t0)
+    sec = statistics.median(secs)
+    parity = "unchecked"
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+            want = [t for t in json.load(f)["tests"] if (t["k"], t["n"]) == (k, n)]
+        if want:
+            ok = (r["verdict"], r["base"], format(r["res64"], "016x")) == (want[0]["verdict"], want[0]["base"],
+                                                                           want[0]["res64"])
+            parity = "ok" if ok else "MISMATCH"
+    except (OSError, KeyError):
+        pass
+    threads = os.cpu_count() or 1
+    cpu = cpu_tests_per_hour([(k, n)] * (2 * threads), cpu_sq)
+    gpu_tph = 3600.0 / sec
+    return {"workload": f"single: k={k}, n={n} (first seed-1 draw past the small-prime gate; "
+                        f"{cands.index((k, n))} earlier draws are gated)",
+            "k": k, "n": n, "fft_len": 1 << lg, "base": r["base"], "verdict": r["verdict"],
+            "res64": format(r["res64"], "016x"), "parity_vs_reference": parity, "status": r["status"],
+            "gerbicz_checks": r["gerbicz_checks"], "seconds_per_test_gpu": sec,
+            "us_per_squaring_gpu": sec * 1e6 / (n - 1 + k.bit_length()),
+            "gpu_tests_per_hour_one_at_a_time": gpu_tph, "shape": _chosen(rows),
+            "cpu": cpu, "gpu_one_at_a_time_over_cpu_all_cores": gpu_tph / cpu["tests_per_hour"],
+            "sample": f"median of {reps} whole tests after one warm-up test"}
+
+
 def uneven_sample(pg, steps=200, warm=50, cpu_sq=60):
     """Uneven batch: 2,048 candidates, n log-uniform in [8192, 262144], k odd < 10^5
     (seed 4), every FFT-length class batched with its autotuned shape.  Per class:
@@ -462,6 +509,7 @@ def run_gpu(args, world, rank, local, pgd):
     eng.close()
     batched = batched_sample(pg) if os.environ.get("PROTH_BENCH_BATCH", "1") == "1" else None
     uneven = uneven_sample(pg) if os.environ.get("PROTH_BENCH_UNEVEN", "1") == "1" else None
+    single = single_sample(pg) if os.environ.get("PROTH_BENCH_SINGLE", "1") == "1" else None
     cpu_ns, cpu_kind, cpu_used, cpu_L = time_cpu_reference(k, n, a, cpu_sample_seconds())
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -494,6 +542,7 @@ def run_gpu(args, world, rank, local, pgd):
         "gpu_launches": launches,
         "batched": batched,
         "batched_uneven": uneven,
+        "single_test": single,
     }
     print(json.dumps(line), flush=True)
     return 0

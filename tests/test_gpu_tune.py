@@ -90,6 +90,34 @@ def test_fused_middle_exact_with_gerbicz(pg, cluster, tpb):
         pg.tune_clear()
 
 
+@pytest.mark.parametrize("when", [30, 250])
+def test_fused_middle_gerbicz_recovers_corruption(pg, gmp, when):
+    """A digit corrupted on the device between squarings of the fused-middle
+    shape (2^15 points, 32*32*32, clusters of 8) is caught by the Gerbicz check;
+    the rollback and the squarings redone through the cluster kernel give the
+    exact residue."""
+    k, n = 1000003, 400000
+    lg = pg.pick_fft_len(k, n).bit_length() - 1
+    assert lg == 15
+    N = k * (1 << n) + 1
+    pg.tune_set(pg.TUNE_ONE, {"lg": lg, "slots": 1, "passes": 3, "f0": 32, "f1": 32, "f2": 32, "g_mid": 2,
+                              "g_inner": 4, "tpb": 1, "cluster": 8})
+    try:
+        with pg.Engine(k, n) as e:
+            e.set_gerbicz(100, 3)
+            e.set_residue(3)
+            e.square(when)
+            e.debug_corrupt(777, 5)
+            e.square(600 - when)
+            assert e.get_residue() == gmp.square_chain(3, 600, N, every=600)[0]
+            assert e.stats()["gerbicz_failures"] >= 1
+        with pg.Engine(k, n) as e:
+            e.set_residue(3)
+            assert e.time_squarings(50)[1] == 3  # the cluster kernel was in use
+    finally:
+        pg.tune_clear()
+
+
 def test_tuned_batch_full_tests_exact(pg, gmp):
     rows = pg.autotune(12, slots=64, iters=50)
     assert any(r["chosen"] for r in rows) and all(r["valid"] for r in rows)
