@@ -307,7 +307,9 @@ def single_sample(pg, reps=3, cpu_sq=1000):
             "gerbicz_checks": r["gerbicz_checks"], "seconds_per_test_gpu": sec,
             "us_per_squaring_gpu": sec * 1e6 / (n - 1 + k.bit_length()),
             "gpu_tests_per_hour_one_at_a_time": gpu_tph, "shape": _chosen(rows),
-            "cpu": cpu, "gpu_one_at_a_time_over_cpu_all_cores": gpu_tph / cpu["tests_per_hour"],
+            "cpu": cpu, "cpu_seconds_per_test_one_core": cpu["cores"] * 3600.0 / cpu["tests_per_hour"],
+            "gpu_over_cpu_per_test": cpu["cores"] * 3600.0 / cpu["tests_per_hour"] / sec,
+            "gpu_one_at_a_time_over_cpu_all_cores": gpu_tph / cpu["tests_per_hour"],
             "sample": f"median of {reps} whole tests after one warm-up test"}
 
 
