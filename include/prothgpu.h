@@ -218,7 +218,7 @@ int pg_batch_set_gerbicz(pg_batch* b, uint64_t block);
 #define PG_TUNE_MANY 1u
 typedef struct pg_tune_result {
     uint32_t lg, slots, passes, f0, f1, f2, g_mid, g_inner;
-    uint32_t tpb;       /* threads per radix-4 butterfly: 1, or 2 (paired lanes, shorter FP64 chains) */
+    uint32_t tpb;       /* threads per radix-4 butterfly: 1, 2 or 4 (lanes sharing it: shorter FP64 chains) */
     uint32_t cluster;   /* one residue, three-pass plans: CTAs of the cluster that runs the middle passes
                            as one kernel (0: three kernels) */
     uint32_t tpb_outer; /* threads per radix-4 butterfly of the first and last passes (0: tpb) */

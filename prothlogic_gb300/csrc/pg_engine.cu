@@ -322,13 +322,15 @@ static void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream
 template <int F0>
 static void launch_first(int tpb, dim3 g, cudaStream_t s, const Slot* sl, int base, const PlanDev& pd,
                          const Slot& one) {
-    if (tpb == 2) launch_pdl(k_first<F0, 2>, g, dim3(4 * F0), s, sl, base, pd, one);
+    if (tpb == 4) launch_pdl(k_first<F0, 4>, g, dim3(8 * F0), s, sl, base, pd, one);
+    else if (tpb == 2) launch_pdl(k_first<F0, 2>, g, dim3(4 * F0), s, sl, base, pd, one);
     else launch_pdl(k_first<F0, 1>, g, dim3(2 * F0), s, sl, base, pd, one);
 }
 template <int F0>
 static void launch_last(int tpb, dim3 g, cudaStream_t s, const Slot* sl, int base, const PlanDev& pd,
                         const Slot& one) {
-    if (tpb == 2) launch_pdl(k_last<F0, 2>, g, dim3(4 * F0), s, sl, base, pd, one);
+    if (tpb == 4) launch_pdl(k_last<F0, 4>, g, dim3(8 * F0), s, sl, base, pd, one);
+    else if (tpb == 2) launch_pdl(k_last<F0, 2>, g, dim3(4 * F0), s, sl, base, pd, one);
     else launch_pdl(k_last<F0, 1>, g, dim3(2 * F0), s, sl, base, pd, one);
 }
 
@@ -340,6 +342,7 @@ static BlockFn block_fn(int F, int CL, int tpb) {
     if (F == FF && CL == CC && tpb == TT) return k_block<FF, CC, TT>;
     PG_BLOCK(64, 4, 1) PG_BLOCK(64, 8, 1) PG_BLOCK(64, 16, 1) PG_BLOCK(64, 4, 2) PG_BLOCK(64, 8, 2)
     PG_BLOCK(64, 16, 2) PG_BLOCK(32, 4, 1) PG_BLOCK(32, 8, 1) PG_BLOCK(32, 4, 2) PG_BLOCK(32, 8, 2)
+    PG_BLOCK(64, 8, 4) PG_BLOCK(64, 16, 4) PG_BLOCK(32, 4, 4) PG_BLOCK(32, 8, 4)
 #undef PG_BLOCK
     return nullptr;
 }
@@ -435,6 +438,8 @@ static int enqueue_step_part(Pool* p, int part, int base, int count, bool solo) 
         PG_INNER2(32, 4, 2, 1) PG_INNER2(32, 8, 2, 1) PG_INNER2(64, 2, 2, 1) PG_INNER2(64, 8, 2, 1)
         PG_INNER2(16, 8, 1, 2) PG_INNER2(32, 4, 1, 2) PG_INNER2(64, 2, 1, 2) PG_INNER2(128, 2, 1, 2)
         PG_INNER2(32, 4, 2, 2) PG_INNER2(64, 2, 2, 2)
+        PG_INNER2(16, 8, 1, 4) PG_INNER2(32, 4, 1, 4) PG_INNER2(64, 2, 1, 4) PG_INNER2(128, 2, 1, 4)
+        PG_INNER2(32, 4, 2, 4) PG_INNER2(64, 2, 2, 4)
 #undef PG_INNER2
     } else {
         if (d.P != 3) return PG_EINVAL;
@@ -445,7 +450,7 @@ static int enqueue_step_part(Pool* p, int part, int base, int count, bool solo) 
         else launch_pdl(k_mid_inv<FF, GG, TT>, gm, dim3(FF * GG / 4 * TT), p->stream, (const Slot*)p->dslots, base, d, one);         \
     }
         PG_MID2(32, 2, 1) PG_MID2(32, 8, 1) PG_MID2(64, 2, 1) PG_MID2(64, 8, 1)
-        PG_MID2(32, 2, 2) PG_MID2(64, 2, 2)
+        PG_MID2(32, 2, 2) PG_MID2(64, 2, 2) PG_MID2(32, 2, 4) PG_MID2(64, 2, 4)
 #undef PG_MID2
     }
     if (part != 0 && part != parts - 1 && nl != 1) return PG_EINVAL;  // no kernel instance for this shape

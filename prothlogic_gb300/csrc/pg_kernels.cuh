@@ -186,16 +186,89 @@ __device__ __forceinline__ void pair_stage_inv(double2* tile, const double2* __r
     tile[ib] = make_double2(u.x - v.x, u.y - v.y);            // Z2 | Z3
 }
 
+__device__ __forceinline__ double2 shfl_xor_d2(double2 v, int m) {
+    return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+// p + q or p - q, the sign chosen per lane without a branch (p - q == p + (-q) exactly).
+__device__ __forceinline__ double add_sgn(double p, double q, bool minus) { return p + (minus ? -q : q); }
+
+// Radix-4 stage s of the forward transform done by FOUR lanes, one input and
+// one output each: lanes (0,2) form a0 +- a2 and lanes (1,3) a1 +- a3 (shuffle
+// over lane distance 2), then lanes (0,1) form y0, y2 and lanes (2,3) y1, y3
+// (distance 1), and each lane multiplies its output by its twiddle.  Every
+// output is the same sum of the same two rounded operands as in bfly4_fwd + cmul
+// (operand selects, no divergent branch), so results are bit-identical; a lane's
+// FP64 chain is 8 instructions per stage, at the price of w^0 = 1 on lane 0.
+template <int F, int G, bool GM>
+__device__ __forceinline__ void quad_stage_fwd(double2* tile, const double2* __restrict__ wF, int tid, int s) {
+    const int sub = tid & 3;
+    const int b = tid >> 2;
+    const int g = b / (F / 4), w = b % (F / 4);
+    const int h = F >> (2 * (s + 1));
+    const int step = F / (4 * h);
+    const int blk = w / h, j = w % h;
+    const int i0 = blk * 4 * h + j;
+    const double2 x = tile[tix<F, G, GM>(g, i0 + sub * h)];
+    const double2 o1 = shfl_xor_d2(x, 2);
+    const bool hi = (sub & 2) != 0;  // lanes 2, 3: other - self
+    const double2 l1 = make_double2(add_sgn(hi ? o1.x : x.x, hi ? x.x : o1.x, hi),
+                                    add_sgn(hi ? o1.y : x.y, hi ? x.y : o1.y, hi));
+    const double2 o2 = shfl_xor_d2(l1, 1);
+    // lane 0: y0 = apc + bpd   lane 1: y2 = apc - bpd   lane 2: y1 = amc - i bmd   lane 3: y3 = amc + i bmd
+    const bool odd = (sub & 1) != 0;
+    const double qx = sub == 0 ? o2.x : sub == 1 ? l1.x : sub == 2 ? o2.y : l1.y;
+    const double qy = sub == 0 ? o2.y : sub == 1 ? l1.y : sub == 2 ? o2.x : l1.x;
+    double2 y = make_double2(add_sgn(odd ? o2.x : l1.x, qx, odd), add_sgn(odd ? o2.y : l1.y, qy, sub == 1 || sub == 2));
+    const int ko = sub == 1 ? 2 : sub == 2 ? 1 : sub;  // output index
+    if (h > 1) y = cmul(y, wF[ko * j * step]);
+    tile[tix<F, G, GM>(g, i0 + ko * h)] = y;
+}
+
+// Inverse counterpart (twiddle on the lane's input, then the two exchanges),
+// bit-identical to cmulc + bfly4_inv.
+template <int F, int G, bool GM>
+__device__ __forceinline__ void quad_stage_inv(double2* tile, const double2* __restrict__ wF, int tid, int s) {
+    const int sub = tid & 3;
+    const int b = tid >> 2;
+    const int g = b / (F / 4), w = b % (F / 4);
+    const int h = F >> (2 * (s + 1));
+    const int step = F / (4 * h);
+    const int blk = w / h, j = w % h;
+    const int i0 = blk * 4 * h + j;
+    double2 x = tile[tix<F, G, GM>(g, i0 + sub * h)];
+    if (h > 1) x = cmulc(x, wF[sub * j * step]);
+    const double2 o1 = shfl_xor_d2(x, 2);
+    const bool hi = (sub & 2) != 0;  // lanes 0, 1: s = z0 + z2, t = z1 + z3; lanes 2, 3: d = z0 - z2, u = z1 - z3
+    const double2 l1 = make_double2(add_sgn(hi ? o1.x : x.x, hi ? x.x : o1.x, hi),
+                                    add_sgn(hi ? o1.y : x.y, hi ? x.y : o1.y, hi));
+    const double2 o2 = shfl_xor_d2(l1, 1);
+    // lane 0: Z0 = s + t   lane 1: Z2 = s - t   lane 2: Z1 = d + i u   lane 3: Z3 = d - i u
+    const bool odd = (sub & 1) != 0;
+    const double qx = sub == 0 ? o2.x : sub == 1 ? l1.x : sub == 2 ? o2.y : l1.y;
+    const double qy = sub == 0 ? o2.y : sub == 1 ? l1.y : sub == 2 ? o2.x : l1.x;
+    const double2 z = make_double2(add_sgn(odd ? o2.x : l1.x, qx, sub == 1 || sub == 2),
+                                   add_sgn(odd ? o2.y : l1.y, qy, odd));
+    const int ko = sub == 1 ? 2 : sub == 2 ? 1 : sub;
+    tile[tix<F, G, GM>(g, i0 + ko * h)] = z;
+}
+
 // In-place forward DFT of length F on G groups of a shared tile, NT threads.
 // Radix-4 stages with spans F/4, F/16, ...; a final radix-2 stage if log2 F is
 // odd.  Output order is the digit reversal that the host's permutation table
 // (plan construction) describes; the inverse below undoes it exactly.  With
-// NT == F*G/2 every radix-4 butterfly is done by a pair of lanes.
+// NT == F*G/2 every radix-4 butterfly is done by a pair of lanes, with
+// NT == F*G by four lanes.
 template <int F, int G, int NT, bool GM, class Sync>
 __device__ __forceinline__ void smem_fft_fwd(double2* tile, const double2* __restrict__ wF, int tid, Sync sync) {
     constexpr int LG = Lg<F>::v;
     constexpr int N4 = LG / 2;
-    if constexpr (NT == F * G / 2) {
+    if constexpr (NT == F * G) {
+#pragma unroll
+        for (int s = 0; s < N4; ++s) {
+            quad_stage_fwd<F, G, GM>(tile, wF, tid, s);
+            sync();
+        }
+    } else if constexpr (NT == F * G / 2) {
 #pragma unroll
         for (int s = 0; s < N4; ++s) {
             pair_stage_fwd<F, G, GM>(tile, wF, tid, s);
@@ -256,7 +329,13 @@ __device__ __forceinline__ void smem_fft_inv(double2* tile, const double2* __res
         }
         sync();
     }
-    if constexpr (NT == F * G / 2) {
+    if constexpr (NT == F * G) {
+#pragma unroll
+        for (int s = N4 - 1; s >= 0; --s) {
+            quad_stage_inv<F, G, GM>(tile, wF, tid, s);
+            sync();
+        }
+    } else if constexpr (NT == F * G / 2) {
 #pragma unroll
         for (int s = N4 - 1; s >= 0; --s) {
             pair_stage_inv<F, G, GM>(tile, wF, tid, s);
