@@ -240,7 +240,47 @@ def _chosen(rows):
     outer = r.get("tpb_outer") or r["tpb"]
     tpb = (f"{r['tpb']} thread(s)/butterfly" if outer == r["tpb"]
            else f"{r['tpb']} thread(s)/butterfly ({outer} in the first and last passes)")
-    return f"{radices} {mid} {tpb} (fastest of {len(rows)} bit-identical shapes)"
+    how = ("fastest in situ of the tuner's three fastest" if "us_in_situ" in r else "fastest")
+    return f"{radices} {mid} {tpb} ({how} of {len(rows)} bit-identical shapes)"
+
+
+def pick_in_situ(pg, rows, k, n, a, blocks, top=3):
+    """The tuner times bare squaring chains.  The engine also squares the Gerbicz
+    verification chain beside the residue in the last block of each interval,
+    and that can rank the fastest few shapes differently: time each of the
+    tuner's `top` fastest shapes on one verified interval of this workload
+    (`blocks` blocks of SQ_PER_STEP squarings, verification included), install
+    the fastest, and mark it chosen in the returned rows."""
+    ok = sorted((r for r in rows if r["valid"]), key=lambda r: r["us_per_step"])[:top]
+    best, best_ms = None, None
+    for r in ok:
+        pg.tune_set(pg.TUNE_ONE, r)
+        with pg.Engine(k, n) as e:
+            e.set_gerbicz(SQ_PER_STEP, blocks)
+            e.set_residue(a)
+            e.square(SQ_PER_STEP)                     # graphs, plans, weights
+            e.set_residue(a)
+            ms = e.square_timed(blocks * SQ_PER_STEP)
+        r["us_in_situ"] = ms * 1e3 / (blocks * SQ_PER_STEP)
+        if best_ms is None or ms < best_ms:
+            best, best_ms = r, ms
+    if best is None:
+        return rows
+    pg.tune_set(pg.TUNE_ONE, best)
+    for r in rows:
+        r["chosen"] = 1 if r is best else 0
+    return rows
+
+
+def _top_shapes(rows, count=5):
+    """The fastest valid shapes as (label, us per squaring), fastest first."""
+    def label(r):
+        radices = "x".join(str(r[f]) for f in ("f0", "f1", "f2")[: r["passes"]])
+        mid = f"cl{r['cluster']}" if r.get("cluster") else f"g{r['g_mid']}/{r['g_inner']}"
+        return f"{radices} {mid} tpb{r['tpb']}/{r.get('tpb_outer') or r['tpb']}"
+    ok = sorted((r for r in rows if r["valid"]), key=lambda r: r["us_per_step"])
+    return [[label(r), round(r["us_per_step"], 2)] + ([round(r["us_in_situ"], 2)] if "us_in_situ" in r else [])
+            for r in ok[:count]]
 
 
 def _chosen_radices(rows):
@@ -422,7 +462,8 @@ def run_gpu(args, world, rank, local, pgd):
     peaks = measured_peaks()
     fp64_tflops = pg.measure_fp64_peak()
     lg = pg.pick_fft_len(k, n).bit_length() - 1
-    tune_rows = pg.autotune(lg, slots=1, iters=200)   # launch shape for one residue at this length
+    tune_rows = pg.autotune(lg, slots=1, iters=400)   # launch shape for one residue at this length
+    tune_rows = pick_in_situ(pg, tune_rows, k, n, a, K)
 
     eng = pg.Engine(k, n)
     M = eng.fft_len
@@ -522,7 +563,10 @@ def run_gpu(args, world, rank, local, pgd):
                    "gerbicz": f"block {SQ_PER_STEP}, {K} blocks verified in the last step",
                    "l2": "flushed between steps (512 MiB write)", "parity_res64": parity,
                    "gerbicz_checks": stats["gerbicz_checks"], "gerbicz_failures": stats["gerbicz_failures"],
-                   "fft_bumps": stats["fft_bumps"], "max_err": max_err, "shape": _chosen(tune_rows)},
+                   "fft_bumps": stats["fft_bumps"], "max_err": max_err, "shape": _chosen(tune_rows),
+                   "shape_candidates_fastest": _top_shapes(tune_rows),
+                   "shape_candidates_columns": "shape, us per squaring in the tuner (bare chain), us per "
+                                               "squaring on a verified interval of this workload"},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved_gbs / hbm_peak if hbm_peak else None, "traffic": traffic,
                      "kernels_live": kernels_live,
