@@ -280,7 +280,7 @@ struct Pool {
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (base, count) -> GSTEPS-step graph
     bool big = false;
     int gm[2] = {2, 2}, gi[2] = {2, 2};  // middle / inner columns per CTA: [0] one residue per launch, [1] many
-    int tpb[2] = {1, 1};                 // threads per radix-4 butterfly (2: paired lanes)
+    int tpb[2] = {1, 1};                 // threads per radix-4 butterfly (2, 4: lanes sharing one)
     int tpb0[2] = {1, 1};                // the same for the first and last passes
     int cl = 0;                          // solo steps: cluster CTAs of the fused middle (k_block), 0: off
     bool capturing = false;

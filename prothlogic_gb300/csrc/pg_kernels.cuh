@@ -819,7 +819,7 @@ __device__ __forceinline__ void tile_last(const Slot& sl, const Slot& pb, const 
 // single residue (blockIdx.y == 0) for a step count the host controls exactly,
 // so the kernels skip the slot-table load and the activity checks.
 
-// TPB: threads per radix-4 butterfly (1, or 2 for the paired-lane transform).
+// TPB: threads per radix-4 butterfly (1; 2 or 4 for the paired- and four-lane transforms).
 template <int F0, int TPB = 1>
 __global__ void __launch_bounds__(2 * F0 * TPB) k_first(const Slot* __restrict__ slots, int base, const PlanDev pl,
                                                         const Slot one) {
