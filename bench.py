@@ -240,6 +240,8 @@ def _chosen(rows):
     outer = r.get("tpb_outer") or r["tpb"]
     tpb = (f"{r['tpb']} thread(s)/butterfly" if outer == r["tpb"]
            else f"{r['tpb']} thread(s)/butterfly ({outer} in the first and last passes)")
+    if r.get("pinned"):
+        return f"{radices} {mid} {tpb} (pinned by PROTH_SHAPE)"
     how = ("fastest in situ of the tuner's three fastest" if "us_in_situ" in r else "fastest")
     return f"{radices} {mid} {tpb} ({how} of {len(rows)} bit-identical shapes)"
 
@@ -462,8 +464,14 @@ def run_gpu(args, world, rank, local, pgd):
     peaks = measured_peaks()
     fp64_tflops = pg.measure_fp64_peak()
     lg = pg.pick_fft_len(k, n).bit_length() - 1
-    tune_rows = pg.autotune(lg, slots=1, iters=400)   # launch shape for one residue at this length
-    tune_rows = pick_in_situ(pg, tune_rows, k, n, a, K)
+    pinned = os.environ.get("PROTH_SHAPE")  # e.g. to rerun a measured shape under ncu (its timings mislead the tuner)
+    if pinned:
+        shape = parse_shape(pinned, lg)
+        pg.tune_set(pg.TUNE_ONE, shape)
+        tune_rows = [dict(shape, us_per_step=0.0, valid=1, chosen=1, pinned=1)]
+    else:
+        tune_rows = pg.autotune(lg, slots=1, iters=400)   # launch shape for one residue at this length
+        tune_rows = pick_in_situ(pg, tune_rows, k, n, a, K)
 
     eng = pg.Engine(k, n)
     M = eng.fft_len
@@ -479,12 +487,20 @@ def run_gpu(args, world, rank, local, pgd):
     pg.flush_l2()
     sampler = ClockSampler(local)
     launches0 = pg.launch_count()
+    nvtx = None
+    if os.environ.get("PROTH_NVTX") == "1":  # name the timed region for an ncu launch list (--nvtx-include timed/)
+        import torch
+        nvtx = torch.cuda.nvtx
     barrier(pgd)
     sampler.start()
+    if nvtx:
+        nvtx.range_push("timed")
     step_ms = []
     for _ in range(K):
         step_ms.append(eng.square_timed(SQ_PER_STEP))
         pg.flush_l2()  # untimed, between steps
+    if nvtx:
+        nvtx.range_pop()
     clocks = sampler.stop()
     launches = pg.launch_count() - launches0 - K  # minus the flush memsets (not counted anyway)
     total_ms = max_over_ranks(pgd, sum(step_ms))
