@@ -1,6 +1,6 @@
 #!/bin/bash
 # Builds the UNMODIFIED reference engine + ref_harness.cpp into oracle/_ref/.
-# Runs only where the reference sources are present (not on the GPU machine) and
+# Runs only where the reference sources are present (an aarch64 host has none) and
 # only on x86-64 with AVX-512 (the reference uses AVX-512 intrinsics and x86 asm).
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
