@@ -131,6 +131,17 @@ def test_tune_set_validates_cluster_shapes():
                      "tpb": 1, "cluster": 8}):                  # two-pass plans have no middle
             with pytest.raises(pg.ProthGpuError):
                 pg.tune_set(pg.TUNE_ONE, bad)
+        # lanes per butterfly: 1, 2 or 4, separately for the first and last passes
+        quad = {"lg": 12, "slots": 1, "passes": 2, "f0": 32, "f1": 128, "f2": 0, "g_mid": 2, "g_inner": 2,
+                "tpb": 2, "tpb_outer": 4}
+        pg.tune_set(pg.TUNE_ONE, quad)
+        got = pg.tune_get(12, pg.TUNE_ONE)
+        assert (got["tpb"], got["tpb_outer"]) == (2, 4)
+        pg.tune_set(pg.TUNE_ONE, dict(quad, tpb=4, tpb_outer=0))
+        assert pg.tune_get(12, pg.TUNE_ONE)["tpb_outer"] == 4  # 0: the same as tpb
+        for bad in (dict(quad, tpb=3), dict(quad, tpb_outer=8), dict(quad, f1=128, g_inner=8, tpb=4)):
+            with pytest.raises(pg.ProthGpuError):
+                pg.tune_set(pg.TUNE_ONE, bad)
     finally:
         pg.tune_clear()
 
