@@ -246,34 +246,6 @@ def _chosen(rows):
     return f"{radices} {mid} {tpb} ({how} of {len(rows)} bit-identical shapes)"
 
 
-def pick_in_situ(pg, rows, k, n, a, blocks, top=3):
-    """The tuner times bare squaring chains.  The engine also squares the Gerbicz
-    verification chain beside the residue in the last block of each interval,
-    and that can rank the fastest few shapes differently: time each of the
-    tuner's `top` fastest shapes on one verified interval of this workload
-    (`blocks` blocks of SQ_PER_STEP squarings, verification included), install
-    the fastest, and mark it chosen in the returned rows."""
-    ok = sorted((r for r in rows if r["valid"]), key=lambda r: r["us_per_step"])[:top]
-    best, best_ms = None, None
-    for r in ok:
-        pg.tune_set(pg.TUNE_ONE, r)
-        with pg.Engine(k, n) as e:
-            e.set_gerbicz(SQ_PER_STEP, blocks)
-            e.set_residue(a)
-            e.square(SQ_PER_STEP)                     # graphs, plans, weights
-            e.set_residue(a)
-            ms = e.square_timed(blocks * SQ_PER_STEP)
-        r["us_in_situ"] = ms * 1e3 / (blocks * SQ_PER_STEP)
-        if best_ms is None or ms < best_ms:
-            best, best_ms = r, ms
-    if best is None:
-        return rows
-    pg.tune_set(pg.TUNE_ONE, best)
-    for r in rows:
-        r["chosen"] = 1 if r is best else 0
-    return rows
-
-
 def _top_shapes(rows, count=5):
     """The fastest valid shapes as (label, us per squaring), fastest first."""
     def label(r):
@@ -470,8 +442,9 @@ def run_gpu(args, world, rank, local, pgd):
         pg.tune_set(pg.TUNE_ONE, shape)
         tune_rows = [dict(shape, us_per_step=0.0, valid=1, chosen=1, pinned=1)]
     else:
-        tune_rows = pg.autotune(lg, slots=1, iters=400)   # launch shape for one residue at this length
-        tune_rows = pick_in_situ(pg, tune_rows, k, n, a, K)
+        # launch shape for one residue at this length: the tuner's three fastest on bare
+        # chains, timed again on one verified interval of this workload (K blocks)
+        tune_rows = pg.autotune_engine(k, n, base=a, blocks=K, block=SQ_PER_STEP, top=3, iters=400)
 
     eng = pg.Engine(k, n)
     M = eng.fft_len

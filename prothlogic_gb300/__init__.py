@@ -17,6 +17,7 @@ __all__ = ["ProthGpuError", "Engine", "Batch", "proth_test", "execute_proth_test
            "load", "pick_fft_len", "gate_rejects", "choose_base", "host_roundtrip", "prefilter"]
 
 PG_OK = 0
+PG_EINVAL = 1
 PG_EROUNDOFF = 3
 PG_EGERBICZ = 4
 PG_ESTATE = 9
@@ -326,6 +327,39 @@ class Engine:
         ci = _u64()
         _check(load().pg_checkpoint_load(self._h, os.fsencode(path), ctypes.byref(ci)), "pg_checkpoint_load")
         return ci.value
+
+
+def autotune_engine(k, n, base=None, blocks=10, block=1000, top=3, iters=400):
+    """Launch shape for engines at the FFT length of k*2^n+1, chosen for the work
+    an engine does.  pg_autotune times every compiled shape on bare squaring
+    chains; its `top` fastest are then timed on one Gerbicz-checked interval of
+    this candidate -- `blocks` blocks of `block` squarings, the verification
+    chain squared beside the residue in the last block, as Engine.square runs
+    it -- and the fastest there is installed for later engines (the two
+    rankings can differ).  Returns the autotune rows: the installed one has
+    "chosen" set, each timed one carries "us_in_situ" (us per squaring)."""
+    lg = pick_fft_len(k, n).bit_length() - 1
+    if lg < 0:
+        raise ProthGpuError(PG_EINVAL, f"autotune_engine(k={k}, n={n}): no FFT length")
+    rows = autotune(lg, slots=1, iters=iters)
+    x0 = base if base else (choose_base(k, n) or 3)  # any residue times the same
+    best = None
+    for r in sorted((r for r in rows if r["valid"]), key=lambda r: r["us_per_step"])[:top]:
+        tune_set(TUNE_ONE, r)
+        with Engine(k, n) as e:
+            e.set_gerbicz(block, blocks)
+            e.set_residue(x0)
+            e.square(block)                       # graphs, plans, weights
+            e.set_residue(x0)
+            ms = e.square_timed(blocks * block)
+        r["us_in_situ"] = ms * 1e3 / (blocks * block)
+        if best is None or r["us_in_situ"] < best["us_in_situ"]:
+            best = r
+    if best is not None:
+        tune_set(TUNE_ONE, best)
+        for r in rows:
+            r["chosen"] = 1 if r is best else 0
+    return rows
 
 
 def proth_test(k, n, flags=0):

@@ -118,6 +118,27 @@ def test_fused_middle_gerbicz_recovers_corruption(pg, gmp, when):
         pg.tune_clear()
 
 
+def test_autotune_engine_picks_on_a_verified_interval(pg, gmp):
+    """autotune_engine times the tuner's fastest shapes on a Gerbicz-checked run
+    of the candidate itself, installs the fastest there, and engines under it are
+    exact."""
+    k, n = 1000003, 400000  # 2^15 points
+    rows = pg.autotune_engine(k, n, blocks=2, block=200, top=2, iters=100)
+    timed = [r for r in rows if "us_in_situ" in r]
+    chosen = [r for r in rows if r["chosen"]]
+    assert len(timed) == 2 and len(chosen) == 1
+    assert chosen[0]["us_in_situ"] == min(r["us_in_situ"] for r in timed)
+    got = pg.tune_get(15, pg.TUNE_ONE)
+    keys = ("passes", "f0", "f1", "f2", "g_mid", "g_inner", "tpb", "tpb_outer", "cluster")
+    assert tuple(got[f] for f in keys) == tuple(chosen[0][f] for f in keys)
+    N = k * (1 << n) + 1
+    with pg.Engine(k, n) as e:
+        e.set_residue(3)
+        e.square(300)
+        assert e.get_residue() == gmp.square_chain(3, 300, N, every=300)[0]
+    pg.tune_clear()
+
+
 def test_tuned_batch_full_tests_exact(pg, gmp):
     rows = pg.autotune(12, slots=64, iters=50)
     assert any(r["chosen"] for r in rows) and all(r["valid"] for r in rows)

@@ -158,3 +158,10 @@ def test_bench_module_helpers():
     label = bench._chosen([row, dict(row, chosen=0)])
     assert label.startswith("64x32x32 middle fused in clusters of 8 CTAs") and "fastest of 2" in label
     assert bench.dp_ops_per_point((16, 64, 64)) == 126
+
+
+def test_autotune_engine_rejects_unsupported_sizes():
+    """autotune_engine refuses a candidate with no FFT length before touching a device."""
+    with pytest.raises(pg.ProthGpuError) as ei:
+        pg.autotune_engine(3, 100)
+    assert ei.value.status == pg.PG_EINVAL
