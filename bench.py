@@ -133,19 +133,30 @@ def dp_ops_per_point(plan_F):
 
 def profile_traffic():
     """(DRAM bytes of one squaring, the launch shape they were captured on) from
-    the committed ncu launch-list summary, or (None, None)."""
-    path = os.path.join(ROOT, "profiles", "squaring_n1048576.md")
-    got, shape = None, None
+    the ncu capture data committed under profiles/, or (None, None)."""
     try:
-        with open(path) as f:
-            for ln in f:
-                if ln.startswith("dram_bytes_per_squaring:"):
-                    got = float(ln.split(":", 1)[1])
-                elif ln.startswith("profiled_shape:"):
-                    shape = ln.split(":", 1)[1].strip()
-    except OSError:
-        pass
-    return got, shape
+        with open(os.path.join(ROOT, "profiles", "squaring_n1048576.json")) as f:
+            d = json.load(f)
+        return float(d["dram_bytes_per_squaring"]), d["profiled_shape"]
+    except (OSError, KeyError, ValueError):
+        return None, None
+
+
+def large_parity(k, a, squarings, residue):
+    """'ok' / 'MISMATCH' for the residue after `squarings` squarings of x0 = a at
+    the n = 2^20 configuration, against the GMP values in tests/golden (RES64
+    every 1,000 squarings up to 200,000); 'unchecked: ...' beyond them."""
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+            g = json.load(f)["large"]
+    except (OSError, KeyError):
+        return "unchecked: golden vector missing"
+    if g["k"] != k or g["a"] != a:
+        return "unchecked: golden vector is for another candidate"
+    if squarings % g["every"] or squarings > len(g["res64"]) * g["every"]:
+        return f"unchecked: {squarings} squarings is beyond the golden vector ({len(g['res64']) * g['every']})"
+    want = g["res64"][squarings // g["every"] - 1]
+    return "ok" if format(residue & ((1 << 64) - 1), "016x") == want else "MISMATCH"
 
 
 def dist_setup():
@@ -178,54 +189,77 @@ def cpu_sample_seconds():
     return float(os.environ.get("PROTH_CPU_SAMPLE_S", "15"))
 
 
-def time_cpu_reference(k, n, a, budget_s, min_sq=4):
-    """Squarings of the reference algorithm on one host core (oracle/_ref on x86-64, else the C oracle port)."""
+def cpu_flags_note():
+    from oracle.build_oracle import bench_flags
+    return " ".join(f for f in bench_flags() if f not in ("-std=c11", "-fPIC", "-shared"))
+
+
+def cpu_reference_setup(k, n):
+    """(callable that times `count` squarings and returns seconds, kind, L, flags):
+    the unmodified reference engine (oracle/_ref) where it was built (x86-64 with
+    AVX-512), else the C restatement built with the reference's optimisation flags."""
     from oracle.build_oracle import build_ref
     from tests import _oracle
-    L = _oracle.lib().ora_choose_L(n, k)
+    fast = _oracle.bench_lib()
+    L = fast.ora_choose_L(n, k)
+    a = int(fast.ora_choose_base(k, n))
     ref = build_ref() if os.environ.get("PROTH_USE_REF", "1") == "1" else None
     if ref:
-        # engine-only microseconds per squaring of the unmodified reference engine
-        steps = max(min_sq, int(budget_s / 0.013))
-        out = subprocess.run([ref, "time", str(k), str(n), str(L), str(steps)], capture_output=True, text=True,
-                             check=True, cwd="/tmp")
-        us = float(out.stdout.strip().splitlines()[-1])
-        return us * 1e3, "reference", steps, L
-    ctx = _oracle.Ctx(L)
+        def run(count):
+            out = subprocess.run([ref, "time", str(k), str(n), str(L), str(count)], capture_output=True, text=True,
+                                 check=True, cwd="/tmp")
+            return float(out.stdout.strip().splitlines()[-1]) * 1e-6 * count
+        return run, "reference", L, "SETUP:25 (-O3 -march=native -mavx512f ... -ffast-math)"
+    ctx = _oracle.Ctx(L, fast)
     x = _oracle.to_limbs(a, L // 4)
-    t0 = time.perf_counter()
-    done = 0
-    while done < min_sq or time.perf_counter() - t0 < budget_s:
-        _oracle.lib().ora_run_squarings(ctx.h, x, n, k, 1)
-        done += 1
-    dt = time.perf_counter() - t0
-    return dt / done * 1e9, "port", done, L
+
+    def run(count):
+        t0 = time.perf_counter()
+        fast.ora_run_squarings(ctx.h, x, n, k, count)
+        return time.perf_counter() - t0
+    run.ctx = ctx  # keeps the context alive
+    return run, "port", L, cpu_flags_note()
+
+
+def time_cpu_reference(k, n, budget_s, min_sq=4):
+    """ns per squaring of the reference algorithm on one host core, over a sample of
+    about budget_s seconds; returns (ns, kind, squarings, L, flags)."""
+    run, kind, L, flags = cpu_reference_setup(k, n)
+    t1 = run(1)
+    count = max(min_sq, int(budget_s / max(t1, 1e-6)))
+    dt = run(count)
+    return dt / count * 1e9, kind, count, L, flags
 
 
 def run_reference(args, world, rank, pgd):
+    """The reference arm: the reference's CPU algorithm for this metric and
+    workload on this host (one thread: the reference's per-candidate engine is
+    single-threaded, SETUP:25 builds it without OpenMP).  Each step times the
+    same bounded sample of squarings; only the oracle library is loaded."""
     if rank != 0:
         return 0
     k, n = workloads.large()
-    import prothlogic_gb300 as pg
-    a = pg.choose_base(k, n)
+    run, kind, L, flags = cpu_reference_setup(k, n)
     per_step_budget = max(0.2, cpu_sample_seconds() / max(1, args.steps + args.warmup))
+    t1 = run(1)
+    sq_per_step = max(1, int(per_step_budget / max(t1, 1e-6)))
     for _ in range(args.warmup):
-        time_cpu_reference(k, n, a, per_step_budget, min_sq=2)
-    vals = []
-    kind, used, L = "port", 0, 0
-    for _ in range(args.steps):
-        ns, kind, used, L = time_cpu_reference(k, n, a, per_step_budget, min_sq=2)
-        vals.append(ns)
-    v = statistics.mean(vals)
+        run(sq_per_step)
+    secs = [run(sq_per_step) for _ in range(args.steps)]
+    v = sum(secs) / (sq_per_step * args.steps) * 1e9
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * SQ_PER_STEP / 1e6,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(secs) * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded candidate, no dataset)",
             "config": {"workload": "large: n=1048576, k odd in [3,2^20) seed 2, x0=a", "k": k, "n": n,
-                       "fft_len_L": L, "squarings_per_step": SQ_PER_STEP},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": kind,
-                             "sample": f"{used} squarings per step at n=1048576, L={L}, one thread "
-                                       "(the reference's per-candidate engine is single-threaded)"},
+                       "fft_len_L": L, "squarings_per_step": sq_per_step,
+                       "step": f"{sq_per_step} squarings of the reference algorithm (a bounded sample; the GPU "
+                               f"arm's step is {SQ_PER_STEP} squarings, the metric is per squaring)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": kind, "flags": flags,
+                             "host_cores": os.cpu_count(),
+                             "sample": f"{sq_per_step} squarings per step x {args.steps} steps at n=1048576, "
+                                       f"L={L}, one thread (the reference's per-candidate engine is "
+                                       "single-threaded)"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -235,11 +269,16 @@ def _chosen(rows):
     """'f0xf1[xf2] g_mid/g_inner (of N shapes)' for the shape the autotuner picked."""
     r = [x for x in rows if x["chosen"]][0]
     radices = "x".join(str(r[f]) for f in ("f0", "f1", "f2")[: r["passes"]])
+    if r.get("resident"):
+        return (f"{radices} resident in shared memory, {r['resident']} CTA(s) x {r['resident_threads']} threads "
+                f"per residue (fastest of {len(rows)} bit-identical shapes)")
     mid = (f"middle fused in clusters of {r['cluster']} CTAs" if r.get("cluster")
            else f"g{r['g_mid']}/{r['g_inner']}")
     outer = r.get("tpb_outer") or r["tpb"]
     tpb = (f"{r['tpb']} thread(s)/butterfly" if outer == r["tpb"]
            else f"{r['tpb']} thread(s)/butterfly ({outer} in the first and last passes)")
+    if r.get("edge"):
+        tpb += ", last+first passes fused"
     if r.get("pinned"):
         return f"{radices} {mid} {tpb} (pinned by PROTH_SHAPE)"
     how = ("fastest in situ of the tuner's three fastest" if "us_in_situ" in r else "fastest")
@@ -250,8 +289,11 @@ def _top_shapes(rows, count=5):
     """The fastest valid shapes as (label, us per squaring), fastest first."""
     def label(r):
         radices = "x".join(str(r[f]) for f in ("f0", "f1", "f2")[: r["passes"]])
+        if r.get("resident"):
+            return f"{radices} res{r['resident']}x{r['resident_threads']}"
         mid = f"cl{r['cluster']}" if r.get("cluster") else f"g{r['g_mid']}/{r['g_inner']}"
-        return f"{radices} {mid} tpb{r['tpb']}/{r.get('tpb_outer') or r['tpb']}"
+        return (f"{radices} {mid} tpb{r['tpb']}/{r.get('tpb_outer') or r['tpb']}"
+                + (" edge" if r.get("edge") else ""))
     ok = sorted((r for r in rows if r["valid"]), key=lambda r: r["us_per_step"])
     return [[label(r), round(r["us_per_step"], 2)] + ([round(r["us_in_situ"], 2)] if "us_in_situ" in r else [])
             for r in ok[:count]]
@@ -274,12 +316,13 @@ def cpu_tests_per_hour(cands, sq_sample, budget_s=None):
     count = len(cands)
     ks = (ctypes.c_uint64 * count)(*[k for k, _ in cands])
     ns = (ctypes.c_uint * count)(*[n for _, n in cands])
-    wall = _oracle.lib().ora_bench_tests(ks, ns, count, threads, sq_sample, None)
+    wall = _oracle.bench_lib().ora_bench_tests(ks, ns, count, threads, sq_sample, None)
     # each test also runs the a^k powering (bitlen(k) - 1 squarings) before its chain
     pow_sq = statistics.mean(max(0, k.bit_length() - 1) for k, _ in cands)
     full = statistics.mean(n - 1 for _, n in cands) + pow_sq
     scale = full / (sq_sample + pow_sq)
     return {"tests_per_hour": count * 3600.0 / (wall * scale), "cores": threads, "kind": "port",
+            "flags": cpu_flags_note(),
             "sample": f"{count} tests on {threads} threads, each truncated to {sq_sample} squarings "
                       f"({wall:.1f} s), scaled by {scale:.0f} to full tests"}
 
@@ -301,16 +344,11 @@ def single_sample(pg, reps=3, cpu_sq=1000):
         r = pg.proth_test(k, n)
         secs.append(time.perf_counter() - t0)
     sec = statistics.median(secs)
+    want = golden_test(k, n)
     parity = "unchecked"
-    try:
-        with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
-            want = [t for t in json.load(f)["tests"] if (t["k"], t["n"]) == (k, n)]
-        if want:
-            ok = (r["verdict"], r["base"], format(r["res64"], "016x")) == (want[0]["verdict"], want[0]["base"],
-                                                                           want[0]["res64"])
-            parity = "ok" if ok else "MISMATCH"
-    except (OSError, KeyError):
-        pass
+    if want is not None:
+        ok = (r["verdict"], r["base"], format(r["res64"], "016x")) == (want["verdict"], want["base"], want["res64"])
+        parity = "ok" if ok else "MISMATCH"
     threads = os.cpu_count() or 1
     cpu = cpu_tests_per_hour([(k, n)] * (2 * threads), cpu_sq)
     gpu_tph = 3600.0 / sec
@@ -325,6 +363,47 @@ def single_sample(pg, reps=3, cpu_sq=1000):
             "gpu_over_cpu_per_test": cpu["cores"] * 3600.0 / cpu["tests_per_hour"] / sec,
             "gpu_one_at_a_time_over_cpu_all_cores": gpu_tph / cpu["tests_per_hour"],
             "sample": f"median of {reps} whole tests after one warm-up test"}
+
+
+def golden_test(k, n):
+    """The reference's own result for the whole test k*2^n+1 (tests/golden), or None."""
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+            g = json.load(f)
+    except OSError:
+        return None
+    return next((t for t in g["tests"] + g["known"] if (t["k"], t["n"]) == (k, n)), None)
+
+
+def shim_sample(pg):
+    """Through the reference's engine API (fft_init / fft_square_karatsuba /
+    fft_destroy) with the reference's own calling pattern: the squaring loop of
+    execute_proth_test_fft (proth_logic.cpp:442-552), one fft_square_karatsuba per
+    squaring on the caller's host limbs at the length auto_tune_fft_len picks
+    (prothlogic_gb300/compat/compat_driver.cpp test).  The whole n = 32,768 test,
+    and a 5,000-squaring sample of 843*2^120002+1."""
+    from prothlogic_gb300 import build as b
+    out = {}
+    for k, n, steps in [(9505, 32768, 0), (843, 120002, 5000)]:
+        L = 256
+        while n / L > 18.0:
+            L *= 2
+        a = pg.choose_base(k, n)
+        x0 = pow(a, k, k * (1 << n) + 1)
+        r = subprocess.run([b.COMPAT_DRIVER, "test", str(k), str(n), str(L), str(steps)], input=format(x0, "x"),
+                           capture_output=True, text=True, check=True).stdout.split()
+        rec = {"k": k, "n": n, "L": L, "squarings": int(r[3]), "us_per_squaring": float(r[4]),
+               "max_err": float(r[5])}
+        if not steps:
+            rec.update(verdict=int(r[1]), res64=r[2])
+            want = golden_test(k, n)
+            rec["parity_vs_reference"] = ("unchecked" if want is None else
+                                          "ok" if (int(r[1]), r[2]) == (want["verdict"], want["res64"])
+                                          else "MISMATCH")
+        out[f"n={n}"] = rec
+    out["note"] = ("per-call path: the caller's limbs go to the device only when changed, the residue comes "
+                   "back after every squaring, Gerbicz blocks of 1,000 verified on schedule")
+    return out
 
 
 def uneven_sample(pg, steps=200, warm=50, cpu_sq=60):
@@ -481,8 +560,8 @@ def run_gpu(args, world, rank, local, pgd):
     res = eng.get_residue()
     max_err = eng.max_err()
     # per-kernel device times of one squaring, kernels launched one by one with
-    # events around each (untimed; serialised like the ncu launch list, so the
-    # shares compare with profiles/squaring_n1048576.md)
+    # events around each (untimed; serialised like an ncu launch list, so the
+    # shares compare with one)
     prof = [eng.profile_step() for _ in range(20)]
     chosen = [r for r in tune_rows if r["chosen"]][0]
     if len(prof[0]) == 5:
@@ -496,15 +575,7 @@ def run_gpu(args, world, rank, local, pgd):
     value = total_ms * 1e6 / (K * SQ_PER_STEP * world)
 
     # parity of the timed run: RES64 after K*1000 squarings of x0 = a (GMP values)
-    parity = "unchecked"
-    try:
-        with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
-            g = json.load(f)["large"]
-        if g["k"] == k and K * SQ_PER_STEP <= len(g["res64"]) * g["every"]:
-            want = g["res64"][K * SQ_PER_STEP // g["every"] - 1]
-            parity = "ok" if format(res & ((1 << 64) - 1), "016x") == want else "MISMATCH"
-    except (OSError, KeyError, IndexError):
-        pass
+    parity = large_parity(k, a, K * SQ_PER_STEP, res)
 
     # e2e through the public API with host buffers: each step is one run of the
     # configuration (set the residue, 10,000 squarings with a Gerbicz check every
@@ -519,9 +590,10 @@ def run_gpu(args, world, rank, local, pgd):
         x = eng.get_residue()
     e2e_s = max_over_ranks(pgd, time.perf_counter() - t0)
     e2e = e2e_s * 1e9 / (K * E2E_SQ_PER_STEP * world)
+    parity_e2e = large_parity(k, a, K * E2E_SQ_PER_STEP, x)
     nl_in = (x.bit_length() + 63) // 64
-    h2d = M * 4 + (M // 8) * 16 + 112          # digits, run carries, slot state
-    d2h = M * 4 + 8 + 112                       # canonical digits, top digit, slot state
+    h2d = M * 4 + (M // 8) * 16 + 128          # digits, run carries, slot state
+    d2h = M * 4 + 8 + 128                       # canonical digits, top digit, slot state
 
     # roofline: algorithmic bytes 32*E per squaring, E = ceil(W/8), W = n + bitlen(k)
     Wbits = n + k.bit_length()
@@ -542,7 +614,8 @@ def run_gpu(args, world, rank, local, pgd):
     batched = batched_sample(pg) if os.environ.get("PROTH_BENCH_BATCH", "1") == "1" else None
     uneven = uneven_sample(pg) if os.environ.get("PROTH_BENCH_UNEVEN", "1") == "1" else None
     single = single_sample(pg) if os.environ.get("PROTH_BENCH_SINGLE", "1") == "1" else None
-    cpu_ns, cpu_kind, cpu_used, cpu_L = time_cpu_reference(k, n, a, cpu_sample_seconds())
+    shim = shim_sample(pg) if os.environ.get("PROTH_BENCH_SHIM", "1") == "1" else None
+    cpu_ns, cpu_kind, cpu_used, cpu_L, cpu_fl = time_cpu_reference(k, n, cpu_sample_seconds())
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": total_ms / K, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
@@ -551,6 +624,7 @@ def run_gpu(args, world, rank, local, pgd):
                    "k": k, "n": n, "base_a": a, "fft_len": M, "squarings_per_step": SQ_PER_STEP,
                    "gerbicz": f"block {SQ_PER_STEP}, {K} blocks verified in the last step",
                    "l2": "flushed between steps (512 MiB write)", "parity_res64": parity,
+                   "parity_res64_e2e": parity_e2e,
                    "gerbicz_checks": stats["gerbicz_checks"], "gerbicz_failures": stats["gerbicz_failures"],
                    "fft_bumps": stats["fft_bumps"], "max_err": max_err, "shape": _chosen(tune_rows),
                    "shape_candidates_fastest": _top_shapes(tune_rows),
@@ -568,8 +642,10 @@ def run_gpu(args, world, rank, local, pgd):
                           "flops_alg_per_squaring": 5 * E * math.log2(E),
                           "achieved_alg_tflops": 5 * E * math.log2(E) / t_sq / 1e12,
                           "fp64_peak_tflops": fp64_tflops},
-        "cpu_baseline": {"value": cpu_ns, "unit": UNIT, "cores": 1, "kind": cpu_kind,
-                         "sample": f"{cpu_used} squarings at n=1048576, L={cpu_L}, one host thread"},
+        "cpu_baseline": {"value": cpu_ns, "unit": UNIT, "cores": 1, "kind": cpu_kind, "flags": cpu_fl,
+                         "host_cores": os.cpu_count(),
+                         "sample": f"{cpu_used} squarings at n=1048576, L={cpu_L}, one host thread (the "
+                                   "reference's per-candidate engine is single-threaded)"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "note": "per step: set_residue (H2D) + 10,000 squarings with a Gerbicz check every 1,000 + "
                         "verified get_residue (D2H)"},
@@ -578,9 +654,42 @@ def run_gpu(args, world, rank, local, pgd):
         "batched": batched,
         "batched_uneven": uneven,
         "single_test": single,
+        "reference_api_loop": shim,
     }
+    line["results"] = compact_results(line)  # last key: the summary survives a truncated tail
     print(json.dumps(line), flush=True)
     return 0
+
+
+def compact_results(line):
+    """The figures of every configuration in a few hundred characters."""
+    def r(x, nd=1):
+        return None if x is None else round(x, nd)
+    out = {"ns_per_squaring_n2^20": r(line["value"], 0), "e2e": r(line["e2e"]["value"], 0),
+           "parity": line["config"]["parity_res64"], "parity_e2e": line["config"]["parity_res64_e2e"],
+           "fp64_frac": r(line["roofline_fp64"]["frac"], 3),
+           "cpu_ns_per_squaring": r(line["cpu_baseline"]["value"], 0)}
+    st = line.get("single_test")
+    if st:
+        out["single_n32768"] = {"us_per_sq": r(st["us_per_squaring_gpu"], 2), "s_per_test": r(st["seconds_per_test_gpu"], 3),
+                                "gpu_tph": r(st["gpu_tests_per_hour_one_at_a_time"], 0),
+                                "cpu_tph_all_cores": r(st["cpu"]["tests_per_hour"], 0), "parity": st["parity_vs_reference"]}
+    for key, name in (("batched", "batched_n65536"), ("batched_uneven", "uneven")):
+        b = line.get(key)
+        if b:
+            out[name] = {"tph": r(b["batched_tests_per_hour"], 0), "one_at_a_time_tph": r(b["one_at_a_time_tests_per_hour"], 0),
+                         "x_one_at_a_time": r(b["batched_over_one_at_a_time"], 2),
+                         "cpu_tph": r(b["cpu_reference_tests_per_hour"], 0), "x_cpu": r(b["batched_over_cpu"], 2)}
+            if "parity" in b:
+                out[name]["parity"] = b["parity"]
+    sh = line.get("reference_api_loop")
+    if sh:
+        out["reference_api_loop_us_per_sq"] = {k: r(v["us_per_squaring"], 1) for k, v in sh.items() if k != "note"}
+        out["reference_api_loop_parity"] = sh["n=32768"].get("parity_vs_reference")
+    sv = line.get("serving")
+    if sv:
+        out["serving"] = sv.get("summary")
+    return out
 
 
 def uneven_full():
@@ -621,12 +730,15 @@ def ncu_batch_target():
 
 
 def parse_shape(spec, lg):
-    """'64x32x32,gm=2,gi=4,tpb=1,cl=8' -> a tune-result dict for 2^lg points."""
+    """'64x32x32,gm=2,gi=4,tpb=1,cl=8' (or '16x128,gi=8,res=16,rnt=128') -> a
+    tune-result dict for 2^lg points."""
     parts = spec.split(",")
     radices = [int(x) for x in parts[0].split("x")]
     shape = {"lg": lg, "slots": 1, "passes": len(radices), "f0": radices[0], "f1": radices[1],
-             "f2": radices[2] if len(radices) > 2 else 0, "g_mid": 2, "g_inner": 2, "tpb": 1, "cluster": 0}
-    names = {"gm": "g_mid", "gi": "g_inner", "tpb": "tpb", "cl": "cluster"}
+             "f2": radices[2] if len(radices) > 2 else 0, "g_mid": 2, "g_inner": 2, "tpb": 1, "cluster": 0,
+             "resident": 0, "resident_threads": 0, "edge": 0}
+    names = {"gm": "g_mid", "gi": "g_inner", "tpb": "tpb", "cl": "cluster", "res": "resident",
+             "rnt": "resident_threads", "edge": "edge", "tpb0": "tpb_outer"}
     for kv in parts[1:]:
         key, val = kv.split("=")
         shape[names[key]] = int(val)

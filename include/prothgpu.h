@@ -92,6 +92,17 @@ int pg_destroy(pg_engine* e);
 int pg_set_residue(pg_engine* e, const uint64_t* limbs, size_t n_limbs);
 /* Canonical x mod N into n_limbs limbs (zero-padded); n_limbs >= ceil((n + 64)/64). */
 int pg_get_residue(pg_engine* e, uint64_t* limbs, size_t n_limbs);
+/* The current residue WITHOUT verifying it first (pg_get_residue verifies):
+ * for callers that read the residue after every squaring, where a
+ * verification per read would redo the squarings since the last verified
+ * residue.  Writes the low n_limbs limbs of x mod N (canonical; the value is
+ * truncated when it needs more limbs, as the reference engine's fixed-size
+ * limb buffer truncates it, fft_engine.cpp:925-983); *needed (optional)
+ * receives the limbs x needs, *unverified (optional) the squarings done since
+ * the last verified residue.  No counterpart in the reference, whose engine
+ * has no verification (its callers read v after every fft_square_karatsuba,
+ * proth_logic.cpp:488-533). */
+int pg_peek_residue(pg_engine* e, uint64_t* limbs, size_t n_limbs, size_t* needed, uint64_t* unverified);
 /* x <- x^(2^iters) mod N.  Each squaring records max |x - round(x)|; above 0.4
  * the engine rolls back to its last verified residue and grows the FFT length.
  * A Gerbicz check covers every block of squarings unless PG_FLAG_NO_GERBICZ. */
@@ -165,7 +176,9 @@ int pg_prefilter(const uint64_t* ks, const uint32_t* ns, size_t count, uint64_t 
  * rejected with PG_ETOOBIG.  The first call on a device (the current device)
  * sets the scratch up, synchronously; make that first call before any stream
  * capture.  All calls share the one array: calls whose work overlaps on the GPU
- * race and give wrong answers, so order them (one stream, or events). */
+ * race and give wrong answers, so order them (one stream, or events).  The
+ * array's device address is looked up once per device: after cudaDeviceReset
+ * the library must be reloaded before this is called again. */
 #define PG_PREFILTER_NOALLOC_MAX_COUNT 65536
 #define PG_PREFILTER_NOALLOC_SCRATCH_BYTES 2654464
 int pg_prefilter_noalloc(const uint64_t* d_ks, const uint32_t* d_ns, size_t count, uint64_t bound,
@@ -222,6 +235,11 @@ typedef struct pg_tune_result {
     uint32_t cluster;   /* one residue, three-pass plans: CTAs of the cluster that runs the middle passes
                            as one kernel (0: three kernels) */
     uint32_t tpb_outer; /* threads per radix-4 butterfly of the first and last passes (0: tpb) */
+    uint32_t resident;  /* two-pass plans: CTAs of the cluster that holds one residue in shared memory for a
+                           whole squaring chain (k_resident; 0: per-pass kernels) */
+    uint32_t resident_threads; /* threads per CTA of that kernel */
+    uint32_t edge;      /* one residue: the last pass of each squaring and the first pass of the next as one
+                           kernel (k_edge), 0 or 1 */
     double us_per_step; /* one squaring of every slot */
     int32_t valid;      /* residues equal to the other shapes', no roundoff or range flag */
     int32_t chosen;

@@ -1,8 +1,19 @@
-"""Build the oracle (test infrastructure, the checker) into oracle/_build/liboracle.so.
+"""Build the oracle (test infrastructure, the checker) into oracle/_build/.
 
-Only tests/, the smoke check and bench.py's CPU-baseline leg load it.
+Only tests/, the smoke check and bench.py's CPU legs load what this builds.
+
+  liboracle.so        the exact checker: gcc -O3, no value-changing flags.
+  liboracle_bench.so  the same C restatement built with the reference's own
+                      optimisation flags (SETUP:25: -O3 -march=native
+                      -funroll-loops -fomit-frame-pointer -ffast-math; on
+                      aarch64 -mcpu=native stands for -march=native, the
+                      AVX-512 flags have no counterpart).  Used only to time
+                      the CPU baseline; tests check that it still reproduces
+                      the reference's residues.
+
 Also builds the reference harness oracle/_ref/ref_harness when the reference
-sources are present and the host is x86-64 (see oracle/ref/build_ref.sh).
+sources are named (PROTH_REF_SRC, or the `src` argument) and the host is
+x86-64 (see oracle/ref/build_ref.sh).
 """
 import os
 import platform
@@ -10,33 +21,61 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
+BENCH_LIB = os.path.join(HERE, "_build", "liboracle_bench.so")
 SRC = os.path.join(HERE, "proth_oracle.c")
 REF_BIN = os.path.join(HERE, "_ref", "ref_harness")
 
+EXACT_FLAGS = ["-O3", "-std=c11", "-fPIC", "-shared", "-Wall"]
+
+
+def bench_flags():
+    """The reference's SETUP:25 optimisation flags, as they apply to this host."""
+    native = "-mcpu=native" if platform.machine() in ("aarch64", "arm64") else "-march=native"
+    return ["-O3", native, "-funroll-loops", "-fomit-frame-pointer", "-ffast-math", "-std=c11", "-fPIC", "-shared"]
+
+
+def _stale(out):
+    deps = [SRC, os.path.join(HERE, "proth_oracle.h"), os.path.abspath(__file__)]
+    return not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(d) for d in deps)
+
+
+def _build(out, flags, force):
+    if not force and not _stale(out):
+        return out
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    tmp = out + ".tmp"
+    subprocess.check_call(["gcc"] + flags + ["-o", tmp, SRC, "-lm", "-lpthread"])
+    os.replace(tmp, out)
+    return out
+
 
 def build_oracle(force=False):
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
-            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "proth_oracle.h"))):
-        return LIB
-    os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    tmp = LIB + ".tmp"
-    subprocess.check_call(["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-Wall", "-o", tmp, SRC,
-                           "-lm", "-lpthread"])
-    os.replace(tmp, LIB)
-    return LIB
+    return _build(LIB, EXACT_FLAGS, force)
 
 
-def build_ref(force=False):
-    """Returns the harness path, or None where the reference cannot be built."""
-    src = os.environ.get("PROTH_REF_SRC", "/root/reference/prothlogic4.2")
+def build_oracle_bench(force=False):
+    return _build(BENCH_LIB, bench_flags(), force)
+
+
+def ref_src(src=None):
+    """Directory of the reference's prothlogic4.2 sources: the argument, else
+    PROTH_REF_SRC, else None."""
+    return src or os.environ.get("PROTH_REF_SRC") or None
+
+
+def build_ref(force=False, src=None):
+    """Returns the harness path, or None where the reference cannot be built
+    (sources not named or absent, or not an x86-64 host)."""
     if os.path.exists(REF_BIN) and not force:
         return REF_BIN
-    if not os.path.isdir(src) or platform.machine() != "x86_64":
+    src = ref_src(src)
+    if not src or not os.path.isdir(src) or platform.machine() != "x86_64":
         return None
-    r = subprocess.run(["bash", os.path.join(HERE, "ref", "build_ref.sh")], capture_output=True, text=True)
+    r = subprocess.run(["bash", os.path.join(HERE, "ref", "build_ref.sh"), src], capture_output=True, text=True)
     return REF_BIN if r.returncode == 0 and os.path.exists(REF_BIN) else None
 
 
 if __name__ == "__main__":
     print(build_oracle(force=True))
+    print(build_oracle_bench(force=True))
     print(build_ref(force=True))

@@ -1,11 +1,15 @@
 #!/bin/bash
 # Builds the UNMODIFIED reference engine + ref_harness.cpp into oracle/_ref/.
-# Runs only where the reference sources are present (an aarch64 host has none) and
-# only on x86-64 with AVX-512 (the reference uses AVX-512 intrinsics and x86 asm).
+#
+#   build_ref.sh <prothlogic4.2 source directory>     (or PROTH_REF_SRC=<dir> build_ref.sh)
+#
+# Needs the reference sources and an x86-64 host with AVX-512 (the reference
+# engine uses AVX-512 intrinsics and x86 inline assembly).
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
-SRC="${PROTH_REF_SRC:-/root/reference/prothlogic4.2}"
+SRC="${1:-$PROTH_REF_SRC}"
 OUT="$HERE/../_ref"
+[ -n "$SRC" ] || { echo "usage: build_ref.sh <reference prothlogic4.2 directory>"; exit 1; }
 [ -d "$SRC" ] || { echo "reference sources not found: $SRC"; exit 1; }
 [ "$(uname -m)" = "x86_64" ] || { echo "reference needs x86-64 (AVX-512)"; exit 1; }
 mkdir -p "$OUT"

@@ -49,7 +49,7 @@ class PgResult(ctypes.Structure):
 class PgTuneResult(ctypes.Structure):
     _fields_ = [("lg", _u32), ("slots", _u32), ("passes", _u32), ("f0", _u32), ("f1", _u32), ("f2", _u32),
                 ("g_mid", _u32), ("g_inner", _u32), ("tpb", _u32), ("cluster", _u32), ("tpb_outer", _u32),
-                ("us_per_step", ctypes.c_double),
+                ("resident", _u32), ("resident_threads", _u32), ("edge", _u32), ("us_per_step", ctypes.c_double),
                 ("valid", _i32), ("chosen", _i32)]
 
     def as_dict(self):
@@ -79,6 +79,7 @@ SIGNATURES = {
     "pg_set_residue": (ctypes.c_int, [_vp, ctypes.POINTER(_u64), _sz]),
     "pg_get_residue": (ctypes.c_int, [_vp, ctypes.POINTER(_u64), _sz]),
     "pg_square": (ctypes.c_int, [_vp, _u64]),
+    "pg_peek_residue": (ctypes.c_int, [_vp, ctypes.POINTER(_u64), _sz, ctypes.POINTER(_sz), ctypes.POINTER(_u64)]),
     "pg_pow_small": (ctypes.c_int, [_vp, _u64, _u64]),
     "pg_max_err": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
     "pg_fft_len": (ctypes.c_int, [_vp, ctypes.POINTER(_u32)]),

@@ -13,7 +13,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libprothgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["pg_engine.cu", "pg_prefilter.cu", "pg_bigint.cpp"]
-DEPS = SOURCES + ["pg_kernels.cuh", "pg_internal.h", "pg_bigint.h", "pg_engine_more.inc", "pg_tune.inc",
+DEPS = SOURCES + ["pg_kernels.cuh", "pg_resident.cuh", "pg_internal.h", "pg_bigint.h", "pg_engine_more.inc", "pg_tune.inc",
                   os.path.join("..", "..", "include", "prothgpu.h")]
 
 

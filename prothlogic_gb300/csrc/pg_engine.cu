@@ -24,6 +24,7 @@
 #include "../../include/prothgpu.h"
 #include "pg_bigint.h"
 #include "pg_kernels.cuh"
+#include "pg_resident.cuh"
 
 namespace pg {
 
@@ -61,6 +62,9 @@ struct Shape {
     int tpb = 1;  // threads per radix-4 butterfly in every kernel of the step ...
     int tpb0 = 0; // ... except the first and last passes when set (one residue per launch)
     int cl = 0;   // one residue: middle passes fused into one cluster kernel of cl CTAs per block (0: three kernels)
+    int res = 0;  // two-pass plans: squaring chains in k_resident, clusters of res CTAs per residue (0: off)
+    int rnt = 0;  // threads per CTA of k_resident
+    int edge = 0; // one residue: squaring i's last pass and i+1's first pass fused in k_edge
 };
 static std::map<std::pair<int, int>, Shape> g_tuned;  // (lg, mode) -> autotuned shape
 
@@ -283,7 +287,12 @@ struct Pool {
     int tpb[2] = {1, 1};                 // threads per radix-4 butterfly (2, 4: lanes sharing one)
     int tpb0[2] = {1, 1};                // the same for the first and last passes
     int cl = 0;                          // solo steps: cluster CTAs of the fused middle (k_block), 0: off
+    int res[2] = {0, 0};                 // squaring chains in k_resident: CTAs per residue (0: per-pass kernels)
+    int rnt[2] = {0, 0};                 // ... and its threads per CTA
     bool capturing = false;
+    int edge = 0;                        // solo chains: last + first passes fused in k_edge
+    long long* eflags = nullptr;         // k_edge carry-ring flags, S x ecols (step counts)
+    int ecols = 0;                       // column tiles of pass 0 (CTAs of k_edge)
     GridBar* bar = nullptr;      // grid barrier of the persistent kernel
     int persist_grid = 0;        // co-resident CTAs for it (0: not available)
 };
@@ -373,6 +382,119 @@ static bool block_fits(int F, int CL, int tpb) {
     return ok;
 }
 
+// ---- squaring chains with the residue resident in shared memory (k_resident) ----
+
+typedef void (*ResFn)(const Slot*, int, const PlanDev, long long);
+struct ResInst {
+    int F0, F1, CL, NT;
+    ResFn fn;
+    size_t smem;
+};
+#define PG_RES(A, B, C, T) {A, B, C, T, k_resident<A, B, C, T>, ResGeom<A, B, C, T>::SMEM},
+static const ResInst kResInst[] = {
+    // one residue per cluster of 4..16 CTAs (lone residues)
+    PG_RES(16, 128, 16, 128) PG_RES(16, 128, 16, 64) PG_RES(32, 64, 8, 256) PG_RES(32, 64, 8, 128)
+    PG_RES(32, 128, 16, 256) PG_RES(32, 128, 16, 128)
+    // one residue per CTA (batches)
+    PG_RES(64, 64, 1, 256) PG_RES(64, 64, 1, 1024)
+};
+#undef PG_RES
+
+static const ResInst* res_find(int F0, int F1, int CL, int NT) {
+    for (const ResInst& r : kResInst)
+        if (r.F0 == F0 && r.F1 == F1 && r.CL == CL && r.NT == NT) return &r;
+    return nullptr;
+}
+
+// Whether the current device can run this instance (shared memory and cluster
+// size attributes set here, once per device and instance).
+static bool res_fits(const ResInst* ri) {
+    if (!ri) return false;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    static std::mutex mu;
+    static std::map<std::pair<int, const ResInst*>, bool> memo;
+    std::lock_guard<std::mutex> lk(mu);
+    const auto key = std::make_pair(dev, ri);
+    auto it = memo.find(key);
+    if (it != memo.end()) return it->second;
+    bool ok = cudaFuncSetAttribute((const void*)ri->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)ri->smem) == cudaSuccess;
+    if (ok && ri->CL > 8)
+        ok = cudaFuncSetAttribute((const void*)ri->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+             cudaSuccess;
+    if (ok) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(ri->CL);
+        cfg.blockDim = dim3(ri->NT);
+        cfg.dynamicSmemBytes = ri->smem;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = ri->CL;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int clusters = 0;
+        ok = cudaOccupancyMaxActiveClusters(&clusters, (const void*)ri->fn, &cfg) == cudaSuccess && clusters > 0;
+    }
+    cudaGetLastError();  // a refused size is an answer, not an error to keep
+    memo[key] = ok;
+    return ok;
+}
+
+// `steps` squarings of each of slots [base, base + count), one cluster each, in one launch.
+static int launch_resident(const ResInst* ri, const Slot* slots, const PlanDev& d, long long steps, int base,
+                           int count, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(count * ri->CL));
+    cfg.blockDim = dim3(ri->NT);
+    cfg.dynamicSmemBytes = ri->smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = ri->CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PG_CK(cudaLaunchKernelEx(&cfg, ri->fn, slots, base, d, steps));
+    return PG_OK;
+}
+
+// The resident instance a pool uses for `count` residues per launch, or null.
+static const ResInst* pool_res(const Pool* p, int count) {
+    const int mode = count <= 2 ? 0 : 1;  // a lone residue, or it with its check chain
+    const PlanDev& d = p->plan->dev;
+    if (!p->res[mode] || d.P != 2) return nullptr;
+    const ResInst* ri = res_find(d.F[0], d.F[1], p->res[mode], p->rnt[mode]);
+    return res_fits(ri) ? ri : nullptr;
+}
+
+// ---- fused last + first passes of a solo chain (k_edge) ----
+
+typedef void (*EdgeFn)(const PlanDev, const Slot, long long*);
+static EdgeFn edge_fn(int F0, int tpb) {
+#define PG_EDGE(FF, TT) \
+    if (F0 == FF && tpb == TT) return k_edge<FF, TT>;
+    PG_EDGE(16, 1) PG_EDGE(16, 2) PG_EDGE(16, 4) PG_EDGE(32, 1) PG_EDGE(32, 2) PG_EDGE(32, 4)
+    PG_EDGE(64, 1) PG_EDGE(64, 2) PG_EDGE(128, 1) PG_EDGE(128, 2)
+#undef PG_EDGE
+    return nullptr;
+}
+
+// Whether a solo chain of this pool runs with k_edge between its squarings.
+static bool pool_edge(const Pool* p, bool solo) {
+    return solo && p->edge && p->eflags && edge_fn(p->plan->dev.F[0], p->tpb0[0]) != nullptr;
+}
+
+// Forget the published steps of the carry ring (a slot's step count went back
+// or was set from the host: old flags could otherwise match a new step).
+static int pool_reset_edges(Pool* p) {
+    if (p->eflags) PG_CK(cudaMemsetAsync(p->eflags, 0xFF, (size_t)p->S * p->ecols * sizeof(long long), p->stream));
+    return PG_OK;
+}
+
 // Kernels per step: first pass, the middle (three kernels, or one fused
 // cluster kernel for a solo step of a pool with cl set), last pass.
 static int step_parts(const Pool* p, bool solo) {
@@ -459,10 +581,52 @@ static int enqueue_step_part(Pool* p, int part, int base, int count, bool solo) 
     return PG_OK;
 }
 
+// k_edge between squarings of solo slot `base`.
+static int enqueue_edge(Pool* p, int base) {
+    const PlanDev& d = p->plan->dev;
+    const EdgeFn fn = edge_fn(d.F[0], p->tpb0[0]);
+    if (!fn) return PG_EINVAL;
+    const Slot one = p->hslots[base];
+    launch_pdl(fn, dim3(p->ecols), dim3(2 * d.F[0] * p->tpb0[0]), p->stream, d, one,
+               p->eflags + (size_t)base * p->ecols);
+    PG_CK(cudaGetLastError());
+    if (!p->capturing) g_launches++;
+    return PG_OK;
+}
+
+// `steps` squarings of slots [base, base + count) as one kernel sequence: for a
+// solo chain with k_edge, first pass, then per squaring its middle and a fused
+// last + first pass (the last squaring ends with the plain last pass); otherwise
+// `steps` whole squarings.
+static int enqueue_chain(Pool* p, int base, int count, long long steps, bool solo) {
+    if (!pool_edge(p, solo) || count != 1) {
+        for (long long i = 0; i < steps; ++i) {
+            const int rc = enqueue_step(p, base, count, solo);
+            if (rc) return rc;
+        }
+        return PG_OK;
+    }
+    const int parts = step_parts(p, true);
+    int rc = enqueue_step_part(p, 0, base, 1, true);
+    for (long long i = 0; i < steps && !rc; ++i) {
+        for (int part = 1; part < parts - 1 && !rc; ++part) rc = enqueue_step_part(p, part, base, 1, true);
+        if (!rc) rc = (i + 1 < steps) ? enqueue_edge(p, base) : enqueue_step_part(p, parts - 1, base, 1, true);
+    }
+    return rc;
+}
+
+// Kernels one chain of `steps` squarings launches.
+static unsigned long long chain_launches(const Pool* p, int count, long long steps, bool solo) {
+    const int parts = step_parts(p, solo);
+    if (!pool_edge(p, solo) || count != 1) return (unsigned long long)steps * parts;
+    return (unsigned long long)steps * (parts - 1) + 1;
+}
+
 static void pool_free(Pool* p) {
     if (!p) return;
     for (auto& kv : p->graphs) cudaGraphExecDestroy(kv.second);
     cudaFree(p->bar);
+    cudaFree(p->eflags);
     for (int s = 0; s < p->S; ++s)
         if (p->slot_n[s]) put_weights(p->slot_n[s], p->M);
     cudaFree(p->digits);
@@ -517,6 +681,9 @@ static int pool_create(int lg, int S, Pool** out, int mode = 0, const Shape* sha
         p->tpb[0] = p->tpb[1] = sh.tpb;
         p->tpb0[0] = p->tpb0[1] = sh.tpb0 ? sh.tpb0 : sh.tpb;
         p->cl = sh.cl;
+        p->res[0] = p->res[1] = sh.res;
+        p->rnt[0] = p->rnt[1] = sh.rnt;
+        p->edge = sh.edge;
     } else {
         std::lock_guard<std::mutex> lk(g_cache_mu);
         for (int m = 0; m < 2; ++m) {
@@ -529,7 +696,12 @@ static int pool_create(int lg, int S, Pool** out, int mode = 0, const Shape* sha
                 p->gi[m] = t.gi;
                 p->tpb[m] = t.tpb;
                 p->tpb0[m] = t.tpb0 ? t.tpb0 : t.tpb;
-                if (m == 0) p->cl = t.cl;
+                p->res[m] = t.res;
+                p->rnt[m] = t.rnt;
+                if (m == 0) {
+                    p->cl = t.cl;
+                    p->edge = t.edge;
+                }
             }
         }
     }
@@ -549,6 +721,11 @@ static int pool_create(int lg, int S, Pool** out, int mode = 0, const Shape* sha
               cudaMallocHost(&p->h_rb_digits, S * M * sizeof(int)) == cudaSuccess &&
               cudaMallocHost(&p->h_rb_top, S * sizeof(long long)) == cudaSuccess &&
               cudaMallocHost(&p->h_st, S * sizeof(SlotState)) == cudaSuccess;
+    if (ok && p->edge && !p->big) {  // engines: the carry-ring flags of k_edge
+        p->ecols = (int)(M / (size_t)plan->dev.F[0] / RUN);
+        ok = cudaMalloc(&p->eflags, (size_t)S * p->ecols * sizeof(long long)) == cudaSuccess &&
+             cudaMemset(p->eflags, 0xFF, (size_t)S * p->ecols * sizeof(long long)) == cudaSuccess;
+    }
     if (!ok) {
         pool_free(p);
         return PG_ENOMEM;
@@ -612,6 +789,7 @@ static int pool_load(Pool* p, int s, const Limbs& x, uint64_t k, unsigned n, con
     p->h_st[s].op = OP_PRODUCT;
     p->h_st[s].partner = s;
     PG_CK(cudaMemcpyAsync(p->st + s, &p->h_st[s], sizeof(SlotState), cudaMemcpyHostToDevice, p->stream));
+    if (pool_reset_edges(p)) return PG_ECUDA;
     PG_CK(cudaStreamSynchronize(p->stream));  // car is a host temporary
     return PG_OK;
 }
@@ -712,7 +890,7 @@ static int pool_run(Pool* p, long long steps, bool use_graph, int base = 0, int 
             PG_CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
             int rc = PG_OK;
             p->capturing = true;
-            for (int i = 0; i < GSTEPS && rc == PG_OK; ++i) rc = enqueue_step(p, base, count, solo);
+            rc = enqueue_chain(p, base, count, GSTEPS, solo);
             p->capturing = false;
             cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
             if (rc) return rc;
@@ -725,15 +903,28 @@ static int pool_run(Pool* p, long long steps, bool use_graph, int base = 0, int 
     while (steps > 0) {
         if (ge && steps >= GSTEPS) {
             PG_CK(cudaGraphLaunch(ge, p->stream));
-            g_launches += (unsigned long long)GSTEPS * step_parts(p, solo);
+            g_launches += chain_launches(p, count, GSTEPS, solo);
             steps -= GSTEPS;
         } else {
-            int rc = enqueue_step(p, base, count, solo);
+            const long long c = ge ? steps : std::min<long long>(steps, GSTEPS);
+            const int rc = enqueue_chain(p, base, count, c, solo);
             if (rc) return rc;
-            steps -= 1;
+            steps -= c;
         }
     }
     return PG_OK;
+}
+
+// Squaring chains of slots [base, base + count) (every slot squares itself, as
+// far as its own step total allows): one k_resident launch when the pool's
+// shape has a resident instance, else the per-pass kernels.
+static int pool_run_sq(Pool* p, long long steps, bool use_graph, int base, int count, bool solo = false) {
+    if (const ResInst* ri = pool_res(p, count)) {
+        const int rc = launch_resident(ri, p->dslots, p->plan->dev, steps, base, count, p->stream);
+        if (!rc && !p->capturing) g_launches++;
+        return rc;
+    }
+    return pool_run(p, steps, use_graph, base, count, solo);
 }
 
 // Graph of GSTEPS solo steps of slot `base` (captured on the pool stream on first use).
@@ -748,7 +939,7 @@ static int solo_graph(Pool* p, int base, cudaGraphExec_t* out) {
     PG_CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
     int rc = PG_OK;
     p->capturing = true;
-    for (int i = 0; i < GSTEPS && rc == PG_OK; ++i) rc = enqueue_step(p, base, 1, true);
+    rc = enqueue_chain(p, base, 1, GSTEPS, true);
     p->capturing = false;
     cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
     if (rc) return rc;
@@ -767,6 +958,7 @@ static int solo_graph(Pool* p, int base, cudaGraphExec_t* out) {
 // verification chain beside the residue).  Returns with the pool stream
 // ordered after both chains.
 static int pool_run_pair(Pool* p, long long steps, int a) {
+    if (pool_res(p, 2)) return pool_run_sq(p, steps, false, a, 2);  // two clusters of one launch
     if (!p->stream2) PG_CK(cudaStreamCreateWithFlags(&p->stream2, cudaStreamNonBlocking));
     cudaGraphExec_t ga = nullptr, gb = nullptr;
     if (steps >= GSTEPS) {
@@ -780,19 +972,19 @@ static int pool_run_pair(Pool* p, long long steps, int a) {
     PG_CK(cudaEventRecord(fork, p->stream));
     PG_CK(cudaStreamWaitEvent(p->stream2, fork, 0));
     int rc = PG_OK;
-    const int parts = step_parts(p, true);
     while (steps > 0 && rc == PG_OK) {
         if (ga && steps >= GSTEPS) {
             if (cudaGraphLaunch(ga, p->stream) != cudaSuccess || cudaGraphLaunch(gb, p->stream2) != cudaSuccess)
                 rc = PG_ECUDA;
-            g_launches += 2ull * GSTEPS * parts;
+            g_launches += 2ull * chain_launches(p, 1, GSTEPS, true);
             steps -= GSTEPS;
         } else {
-            rc = enqueue_step(p, a, 1, true);
-            std::swap(p->stream, p->stream2);  // the second chain's step goes to the second stream
-            if (!rc) rc = enqueue_step(p, a + 1, 1, true);
+            const long long c = ga ? steps : std::min<long long>(steps, GSTEPS);
+            rc = enqueue_chain(p, a, 1, c, true);
+            std::swap(p->stream, p->stream2);  // the second chain goes to the second stream
+            if (!rc) rc = enqueue_chain(p, a + 1, 1, c, true);
             std::swap(p->stream, p->stream2);
-            steps -= 1;
+            steps -= c;
         }
     }
     cudaEventRecord(join, p->stream2);
@@ -839,6 +1031,18 @@ __global__ void k_copy_state(const Slot* __restrict__ slots, int src, int dst) {
         s.op = OP_PRODUCT;
         s.partner = dst;
         *slots[dst].st = s;
+    }
+}
+
+// Arm slot s for `c` more squarings of its own: total = step + c, roundoff
+// record cleared (the host need not read the step count first).
+__global__ void k_arm(const Slot* __restrict__ slots, int s, long long c) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        SlotState* st = slots[s].st;
+        st->total = st->step + c;
+        st->maxerr_bits = 0;
+        st->op = OP_PRODUCT;
+        st->partner = s;
     }
 }
 
@@ -909,6 +1113,7 @@ static int slot_state(pg_engine* e, int s, SlotState* out) {
 
 static int slot_write(pg_engine* e, int s, const SlotState& st) {
     Pool* p = e->pool;
+    if (pool_reset_edges(p)) return PG_ECUDA;
     p->h_st[s] = st;
     PG_CK(cudaMemcpyAsync(p->st + s, p->h_st + s, sizeof(SlotState), cudaMemcpyHostToDevice, p->stream));
     PG_CK(cudaStreamSynchronize(p->stream));  // the pinned staging entry is reused
@@ -918,6 +1123,7 @@ static int slot_write(pg_engine* e, int s, const SlotState& st) {
 static int slot_copy(pg_engine* e, int src, int dst) {
     if (src == dst) return PG_OK;
     Pool* p = e->pool;
+    if (pool_reset_edges(p)) return PG_ECUDA;
     const size_t M = p->M, nruns = M / RUN;
     PG_CK(cudaMemcpyAsync(p->hslots[dst].digits, p->hslots[src].digits, M * sizeof(int), cudaMemcpyDeviceToDevice,
                           p->stream));
@@ -939,6 +1145,7 @@ static int slot_snapshot(pg_engine* e, int s, bool restore) {
         PG_CK(cudaMemcpyAsync(e->snap_carries, sl.carries, nruns * 2 * sizeof(long long), kind, p->stream));
         PG_CK(cudaMemcpyAsync(e->snap_st, sl.st, sizeof(SlotState), kind, p->stream));
     } else {
+        if (pool_reset_edges(p)) return PG_ECUDA;
         PG_CK(cudaMemcpyAsync(sl.digits, e->snap_digits, M * sizeof(int), kind, p->stream));
         PG_CK(cudaMemcpyAsync(sl.carries, e->snap_carries, nruns * 2 * sizeof(long long), kind, p->stream));
         PG_CK(cudaMemcpyAsync(sl.st, e->snap_st, sizeof(SlotState), kind, p->stream));
@@ -978,54 +1185,50 @@ static int run_squarings(pg_engine* e, int s, uint64_t steps, int count = 1) {
     const uint64_t CHUNK = 2000;
     int guard = 0;
     while (steps > 0) {
+        Pool* p = e->pool;  // (a bump replaces the pool)
         const uint64_t c = std::min<uint64_t>(steps, CHUNK);
         int rc = PG_OK;
-        std::vector<SlotState> st(count);
-        for (int i = 0; i < count && !rc; ++i) rc = slot_state(e, s + i, &st[i]);
-        if (!rc && count == 1) rc = slot_snapshot(e, s, false);
+        if (count == 1) rc = slot_snapshot(e, s, false);
         if (rc) return rc;
-        for (int i = 0; i < count && !rc; ++i) {
-            st[i].total = st[i].step + (long long)c;
-            st[i].maxerr_bits = 0;
-            st[i].op = OP_PRODUCT;
-            st[i].partner = s + i;
-            rc = slot_write(e, s + i, st[i]);
+        for (int i = 0; i < count; ++i) {
+            k_arm<<<1, 32, 0, p->stream>>>(p->dslots, s + i, (long long)c);
+            PG_CK(cudaGetLastError());
+            g_launches++;
         }
-        if (rc) return rc;
         // the cooperative kernel is only used for one residue: its first run on
         // two residues did not finish within the time limit and stays disabled
-        if (e->persist && count == 1 && persist_prepare(e->pool)) {
-            rc = pool_run_persist(e->pool, (long long)c, s, count);
+        if (e->persist && count == 1 && persist_prepare(p)) {
+            rc = pool_run_persist(p, (long long)c, s, count);
             if (rc == PG_ETIMEOUT) {
                 // a barrier wait ran out: stay on the per-pass kernels from now on
                 e->persist = false;
-                if (count != 1) return PG_EROUNDOFF;
                 rc = slot_snapshot(e, s, true);
                 if (rc) return rc;
-                PG_CK(cudaStreamSynchronize(e->pool->stream));
+                PG_CK(cudaStreamSynchronize(p->stream));
                 continue;
             }
         } else if (count == 2 && !(e->flags & PG_FLAG_NO_GRAPH)) {
-            rc = pool_run_pair(e->pool, (long long)c, s);
+            rc = pool_run_pair(p, (long long)c, s);
         } else {
-            rc = pool_run(e->pool, (long long)c, !(e->flags & PG_FLAG_NO_GRAPH), s, count, count == 1);
+            rc = pool_run_sq(p, (long long)c, !(e->flags & PG_FLAG_NO_GRAPH), s, count, count == 1);
         }
         if (rc) return rc;
+        // one read-back of the states of the run: roundoff, range flags, steps done
+        PG_CK(cudaMemcpyAsync(p->h_st + s, p->st + s, count * sizeof(SlotState), cudaMemcpyDeviceToHost, p->stream));
+        PG_CK(cudaStreamSynchronize(p->stream));
         bool bad = false;
         double err = 0.0;
-        for (int i = 0; i < count && !rc; ++i) {
-            SlotState after;
-            rc = slot_state(e, s + i, &after);
+        for (int i = 0; i < count; ++i) {
+            const SlotState& after = p->h_st[s + i];
             const double ei = bits_to_double(after.maxerr_bits);
             err = std::max(err, ei);
-            bad = bad || ei > 0.4 || after.flags != 0 || after.step != st[i].total;
+            bad = bad || ei > 0.4 || after.flags != 0 || after.step != after.total;
         }
-        if (rc) return rc;
         if (bad) {
             if (count == 1) {
                 rc = slot_snapshot(e, s, true);
                 if (rc) return rc;
-                PG_CK(cudaStreamSynchronize(e->pool->stream));
+                PG_CK(cudaStreamSynchronize(p->stream));
             }
             rc = engine_bump(e);
             if (rc) return rc;
@@ -1382,6 +1585,21 @@ int pg_get_residue(pg_engine* e, uint64_t* limbs, size_t n_limbs) {
     return PG_OK;
 }
 
+int pg_peek_residue(pg_engine* e, uint64_t* limbs, size_t n_limbs, size_t* needed, uint64_t* unverified) {
+    if (!e || (!limbs && n_limbs)) return PG_EINVAL;
+    if (!e->loaded) return PG_ESTATE;
+    int rc = pool_readback(e->pool, SX, 1);
+    if (rc) return rc;
+    const Limbs x = slot_value(e->pool, SX);
+    if (needed) *needed = x.size();
+    if (unverified) *unverified = (e->gz && e->armed) ? e->blocks * e->B + e->in_block : 0;
+    if (n_limbs) {
+        memset(limbs, 0, n_limbs * sizeof(uint64_t));
+        std::copy(x.begin(), x.begin() + std::min(x.size(), n_limbs), limbs);
+    }
+    return PG_OK;
+}
+
 int pg_square(pg_engine* e, uint64_t iters) {
     if (!e) return PG_EINVAL;
     if (!e->loaded) return PG_ESTATE;
@@ -1487,7 +1705,7 @@ int pg_time_squarings(pg_engine* e, uint64_t iters, double* ms, uint32_t* kernel
     if (e->persist && persist_prepare(e->pool))
         rc = pool_run_persist(e->pool, (long long)iters, SX, 1);
     else
-        rc = pool_run(e->pool, (long long)iters, !(e->flags & PG_FLAG_NO_GRAPH), SX, 1, true);
+        rc = pool_run_sq(e->pool, (long long)iters, !(e->flags & PG_FLAG_NO_GRAPH), SX, 1, true);
     PG_CK(cudaEventRecord(b, e->pool->stream));
     PG_CK(cudaEventSynchronize(b));
     float f = 0.f;

@@ -38,6 +38,9 @@ struct SlotState {
     long long pend_hi;               //   s*top_a*top_b of the last product, or the re-armed top
     int op;                          // OP_PRODUCT or OP_FORWARD
     int partner;                     // slot whose digits/spectrum multiply this one (self: square)
+    long long tope[2];               // the top digit again, indexed by the parity of the step count it
+                                     //   belongs to: a fused last+first pass (k_edge) reads one entry
+                                     //   while its first CTA writes the other
 };
 
 enum SlotOp : int {
@@ -45,7 +48,7 @@ enum SlotOp : int {
     OP_FORWARD = 1   // operand of another slot's product: fix up + forward passes only
 };
 
-enum SlotFlags : int { SF_DIGIT_OVERFLOW = 1, SF_ROUND_RANGE = 2, SF_WAIT_TIMEOUT = 4 };
+enum SlotFlags : int { SF_DIGIT_OVERFLOW = 1, SF_ROUND_RANGE = 2, SF_WAIT_TIMEOUT = 4, SF_COPY_ABANDONED = 8 };
 
 // Per-slot descriptor (device memory, read-only during a step).
 struct Slot {

@@ -117,10 +117,13 @@ struct PdlFirst {
     }
 };
 
-// Element (group g, index i) of a shared-memory tile.
-template <int F, int G, bool GROUP_MAJOR>
+// Element (group g, index i) of a shared-memory tile.  ST: the row stride in
+// elements (0: dense, F for group-major tiles, G otherwise); a padded stride
+// keeps the strided accesses of a column transform off a single bank.
+template <int F, int G, bool GROUP_MAJOR, int ST = 0>
 __device__ __forceinline__ int tix(int g, int i) {
-    return GROUP_MAJOR ? g * F + i : i * G + g;
+    constexpr int S = ST ? ST : (GROUP_MAJOR ? F : G);
+    return GROUP_MAJOR ? g * S + i : i * S + g;
 }
 
 // Radix-4 stage s of the forward transform done by a PAIR of adjacent lanes:
@@ -130,7 +133,7 @@ __device__ __forceinline__ int tix(int g, int i) {
 // order are those of bfly4_fwd + cmul, so the results are bit-identical to the
 // one-thread butterfly; each lane's FP64 chain is 16 instructions instead of 28,
 // at the price of a multiplication by w^0 = 1 (exact) on lane 0.
-template <int F, int G, bool GM>
+template <int F, int G, bool GM, int ST = 0>
 __device__ __forceinline__ void pair_stage_fwd(double2* tile, const double2* __restrict__ wF, int tid, int s) {
     const int sub = tid & 1;
     const int b = tid >> 1;
@@ -139,7 +142,7 @@ __device__ __forceinline__ void pair_stage_fwd(double2* tile, const double2* __r
     const int step = F / (4 * h);
     const int blk = w / h, j = w % h;
     const int i0 = blk * 4 * h + j;
-    const int ia = tix<F, G, GM>(g, i0 + sub * h), ib = tix<F, G, GM>(g, i0 + (sub + 2) * h);
+    const int ia = tix<F, G, GM, ST>(g, i0 + sub * h), ib = tix<F, G, GM, ST>(g, i0 + (sub + 2) * h);
     const double2 xa = tile[ia], xb = tile[ib];
     const double2 p = make_double2(xa.x + xb.x, xa.y + xb.y);
     const double2 m = make_double2(xa.x - xb.x, xa.y - xb.y);
@@ -160,7 +163,7 @@ __device__ __forceinline__ void pair_stage_fwd(double2* tile, const double2* __r
 
 // Inverse counterpart (twiddles on the inputs, then bfly4_inv), bit-identical
 // to the one-thread butterfly.
-template <int F, int G, bool GM>
+template <int F, int G, bool GM, int ST = 0>
 __device__ __forceinline__ void pair_stage_inv(double2* tile, const double2* __restrict__ wF, int tid, int s) {
     const int sub = tid & 1;
     const int b = tid >> 1;
@@ -169,7 +172,7 @@ __device__ __forceinline__ void pair_stage_inv(double2* tile, const double2* __r
     const int step = F / (4 * h);
     const int blk = w / h, j = w % h;
     const int i0 = blk * 4 * h + j;
-    const int ia = tix<F, G, GM>(g, i0 + sub * h), ib = tix<F, G, GM>(g, i0 + (sub + 2) * h);
+    const int ia = tix<F, G, GM, ST>(g, i0 + sub * h), ib = tix<F, G, GM, ST>(g, i0 + (sub + 2) * h);
     double2 za = tile[ia], zb = tile[ib];
     if (h > 1) {
         const int e = j * step;
@@ -199,7 +202,7 @@ __device__ __forceinline__ double add_sgn(double p, double q, bool minus) { retu
 // output is the same sum of the same two rounded operands as in bfly4_fwd + cmul
 // (operand selects, no divergent branch), so results are bit-identical; a lane's
 // FP64 chain is 8 instructions per stage, at the price of w^0 = 1 on lane 0.
-template <int F, int G, bool GM>
+template <int F, int G, bool GM, int ST = 0>
 __device__ __forceinline__ void quad_stage_fwd(double2* tile, const double2* __restrict__ wF, int tid, int s) {
     const int sub = tid & 3;
     const int b = tid >> 2;
@@ -208,7 +211,7 @@ __device__ __forceinline__ void quad_stage_fwd(double2* tile, const double2* __r
     const int step = F / (4 * h);
     const int blk = w / h, j = w % h;
     const int i0 = blk * 4 * h + j;
-    const double2 x = tile[tix<F, G, GM>(g, i0 + sub * h)];
+    const double2 x = tile[tix<F, G, GM, ST>(g, i0 + sub * h)];
     const double2 o1 = shfl_xor_d2(x, 2);
     const bool hi = (sub & 2) != 0;  // lanes 2, 3: other - self
     const double2 l1 = make_double2(add_sgn(hi ? o1.x : x.x, hi ? x.x : o1.x, hi),
@@ -221,12 +224,12 @@ __device__ __forceinline__ void quad_stage_fwd(double2* tile, const double2* __r
     double2 y = make_double2(add_sgn(odd ? o2.x : l1.x, qx, odd), add_sgn(odd ? o2.y : l1.y, qy, sub == 1 || sub == 2));
     const int ko = sub == 1 ? 2 : sub == 2 ? 1 : sub;  // output index
     if (h > 1) y = cmul(y, wF[ko * j * step]);
-    tile[tix<F, G, GM>(g, i0 + ko * h)] = y;
+    tile[tix<F, G, GM, ST>(g, i0 + ko * h)] = y;
 }
 
 // Inverse counterpart (twiddle on the lane's input, then the two exchanges),
 // bit-identical to cmulc + bfly4_inv.
-template <int F, int G, bool GM>
+template <int F, int G, bool GM, int ST = 0>
 __device__ __forceinline__ void quad_stage_inv(double2* tile, const double2* __restrict__ wF, int tid, int s) {
     const int sub = tid & 3;
     const int b = tid >> 2;
@@ -235,7 +238,7 @@ __device__ __forceinline__ void quad_stage_inv(double2* tile, const double2* __r
     const int step = F / (4 * h);
     const int blk = w / h, j = w % h;
     const int i0 = blk * 4 * h + j;
-    double2 x = tile[tix<F, G, GM>(g, i0 + sub * h)];
+    double2 x = tile[tix<F, G, GM, ST>(g, i0 + sub * h)];
     if (h > 1) x = cmulc(x, wF[sub * j * step]);
     const double2 o1 = shfl_xor_d2(x, 2);
     const bool hi = (sub & 2) != 0;  // lanes 0, 1: s = z0 + z2, t = z1 + z3; lanes 2, 3: d = z0 - z2, u = z1 - z3
@@ -249,7 +252,7 @@ __device__ __forceinline__ void quad_stage_inv(double2* tile, const double2* __r
     const double2 z = make_double2(add_sgn(odd ? o2.x : l1.x, qx, sub == 1 || sub == 2),
                                    add_sgn(odd ? o2.y : l1.y, qy, odd));
     const int ko = sub == 1 ? 2 : sub == 2 ? 1 : sub;
-    tile[tix<F, G, GM>(g, i0 + ko * h)] = z;
+    tile[tix<F, G, GM, ST>(g, i0 + ko * h)] = z;
 }
 
 // In-place forward DFT of length F on G groups of a shared tile, NT threads.
@@ -258,20 +261,20 @@ __device__ __forceinline__ void quad_stage_inv(double2* tile, const double2* __r
 // (plan construction) describes; the inverse below undoes it exactly.  With
 // NT == F*G/2 every radix-4 butterfly is done by a pair of lanes, with
 // NT == F*G by four lanes.
-template <int F, int G, int NT, bool GM, class Sync>
+template <int F, int G, int NT, bool GM, int ST = 0, class Sync>
 __device__ __forceinline__ void smem_fft_fwd(double2* tile, const double2* __restrict__ wF, int tid, Sync sync) {
     constexpr int LG = Lg<F>::v;
     constexpr int N4 = LG / 2;
     if constexpr (NT == F * G) {
 #pragma unroll
         for (int s = 0; s < N4; ++s) {
-            quad_stage_fwd<F, G, GM>(tile, wF, tid, s);
+            quad_stage_fwd<F, G, GM, ST>(tile, wF, tid, s);
             sync();
         }
     } else if constexpr (NT == F * G / 2) {
 #pragma unroll
         for (int s = 0; s < N4; ++s) {
-            pair_stage_fwd<F, G, GM>(tile, wF, tid, s);
+            pair_stage_fwd<F, G, GM, ST>(tile, wF, tid, s);
             sync();
         }
     } else {
@@ -283,10 +286,10 @@ __device__ __forceinline__ void smem_fft_fwd(double2* tile, const double2* __res
             const int g = b / (F / 4), w = b % (F / 4);
             const int blk = w / h, j = w % h;
             const int i0 = blk * 4 * h + j;
-            double2 a0 = tile[tix<F, G, GM>(g, i0)];
-            double2 a1 = tile[tix<F, G, GM>(g, i0 + h)];
-            double2 a2 = tile[tix<F, G, GM>(g, i0 + 2 * h)];
-            double2 a3 = tile[tix<F, G, GM>(g, i0 + 3 * h)];
+            double2 a0 = tile[tix<F, G, GM, ST>(g, i0)];
+            double2 a1 = tile[tix<F, G, GM, ST>(g, i0 + h)];
+            double2 a2 = tile[tix<F, G, GM, ST>(g, i0 + 2 * h)];
+            double2 a3 = tile[tix<F, G, GM, ST>(g, i0 + 3 * h)];
             bfly4_fwd(a0, a1, a2, a3);
             if (h > 1) {
                 const int e = j * step;
@@ -294,10 +297,10 @@ __device__ __forceinline__ void smem_fft_fwd(double2* tile, const double2* __res
                 a2 = cmul(a2, wF[2 * e]);
                 a3 = cmul(a3, wF[3 * e]);
             }
-            tile[tix<F, G, GM>(g, i0)] = a0;
-            tile[tix<F, G, GM>(g, i0 + h)] = a1;
-            tile[tix<F, G, GM>(g, i0 + 2 * h)] = a2;
-            tile[tix<F, G, GM>(g, i0 + 3 * h)] = a3;
+            tile[tix<F, G, GM, ST>(g, i0)] = a0;
+            tile[tix<F, G, GM, ST>(g, i0 + h)] = a1;
+            tile[tix<F, G, GM, ST>(g, i0 + 2 * h)] = a2;
+            tile[tix<F, G, GM, ST>(g, i0 + 3 * h)] = a3;
         }
         sync();
     }
@@ -305,40 +308,40 @@ __device__ __forceinline__ void smem_fft_fwd(double2* tile, const double2* __res
     if (LG & 1) {
         for (int b = tid; b < G * F / 2; b += NT) {
             const int g = b / (F / 2), i0 = 2 * (b % (F / 2));
-            const double2 a = tile[tix<F, G, GM>(g, i0)];
-            const double2 c = tile[tix<F, G, GM>(g, i0 + 1)];
-            tile[tix<F, G, GM>(g, i0)] = make_double2(a.x + c.x, a.y + c.y);
-            tile[tix<F, G, GM>(g, i0 + 1)] = make_double2(a.x - c.x, a.y - c.y);
+            const double2 a = tile[tix<F, G, GM, ST>(g, i0)];
+            const double2 c = tile[tix<F, G, GM, ST>(g, i0 + 1)];
+            tile[tix<F, G, GM, ST>(g, i0)] = make_double2(a.x + c.x, a.y + c.y);
+            tile[tix<F, G, GM, ST>(g, i0 + 1)] = make_double2(a.x - c.x, a.y - c.y);
         }
         sync();
     }
 }
 
 // Exact inverse (times F) of smem_fft_fwd.
-template <int F, int G, int NT, bool GM, class Sync>
+template <int F, int G, int NT, bool GM, int ST = 0, class Sync>
 __device__ __forceinline__ void smem_fft_inv(double2* tile, const double2* __restrict__ wF, int tid, Sync sync) {
     constexpr int LG = Lg<F>::v;
     constexpr int N4 = LG / 2;
     if (LG & 1) {
         for (int b = tid; b < G * F / 2; b += NT) {
             const int g = b / (F / 2), i0 = 2 * (b % (F / 2));
-            const double2 a = tile[tix<F, G, GM>(g, i0)];
-            const double2 c = tile[tix<F, G, GM>(g, i0 + 1)];
-            tile[tix<F, G, GM>(g, i0)] = make_double2(a.x + c.x, a.y + c.y);
-            tile[tix<F, G, GM>(g, i0 + 1)] = make_double2(a.x - c.x, a.y - c.y);
+            const double2 a = tile[tix<F, G, GM, ST>(g, i0)];
+            const double2 c = tile[tix<F, G, GM, ST>(g, i0 + 1)];
+            tile[tix<F, G, GM, ST>(g, i0)] = make_double2(a.x + c.x, a.y + c.y);
+            tile[tix<F, G, GM, ST>(g, i0 + 1)] = make_double2(a.x - c.x, a.y - c.y);
         }
         sync();
     }
     if constexpr (NT == F * G) {
 #pragma unroll
         for (int s = N4 - 1; s >= 0; --s) {
-            quad_stage_inv<F, G, GM>(tile, wF, tid, s);
+            quad_stage_inv<F, G, GM, ST>(tile, wF, tid, s);
             sync();
         }
     } else if constexpr (NT == F * G / 2) {
 #pragma unroll
         for (int s = N4 - 1; s >= 0; --s) {
-            pair_stage_inv<F, G, GM>(tile, wF, tid, s);
+            pair_stage_inv<F, G, GM, ST>(tile, wF, tid, s);
             sync();
         }
     } else {
@@ -350,10 +353,10 @@ __device__ __forceinline__ void smem_fft_inv(double2* tile, const double2* __res
             const int g = b / (F / 4), w = b % (F / 4);
             const int blk = w / h, j = w % h;
             const int i0 = blk * 4 * h + j;
-            double2 z0 = tile[tix<F, G, GM>(g, i0)];
-            double2 z1 = tile[tix<F, G, GM>(g, i0 + h)];
-            double2 z2 = tile[tix<F, G, GM>(g, i0 + 2 * h)];
-            double2 z3 = tile[tix<F, G, GM>(g, i0 + 3 * h)];
+            double2 z0 = tile[tix<F, G, GM, ST>(g, i0)];
+            double2 z1 = tile[tix<F, G, GM, ST>(g, i0 + h)];
+            double2 z2 = tile[tix<F, G, GM, ST>(g, i0 + 2 * h)];
+            double2 z3 = tile[tix<F, G, GM, ST>(g, i0 + 3 * h)];
             if (h > 1) {
                 const int e = j * step;
                 z1 = cmulc(z1, wF[e]);
@@ -361,10 +364,10 @@ __device__ __forceinline__ void smem_fft_inv(double2* tile, const double2* __res
                 z3 = cmulc(z3, wF[3 * e]);
             }
             bfly4_inv(z0, z1, z2, z3);
-            tile[tix<F, G, GM>(g, i0)] = z0;
-            tile[tix<F, G, GM>(g, i0 + h)] = z1;
-            tile[tix<F, G, GM>(g, i0 + 2 * h)] = z2;
-            tile[tix<F, G, GM>(g, i0 + 3 * h)] = z3;
+            tile[tix<F, G, GM, ST>(g, i0)] = z0;
+            tile[tix<F, G, GM, ST>(g, i0 + h)] = z1;
+            tile[tix<F, G, GM, ST>(g, i0 + 2 * h)] = z2;
+            tile[tix<F, G, GM, ST>(g, i0 + 3 * h)] = z3;
         }
         sync();
     }
@@ -522,6 +525,7 @@ __device__ __forceinline__ void tile_first(const Slot& sl, const PlanDev& pl, in
         // the top as pending, so a slot that only feeds another product stays exact
         if (run == 0) {
             st->top = new_top;
+            st->tope[(st->step + 1) & 1] = new_top;  // for a following k_edge (step + 1 by then)
             store_pend(st, (i128)new_top);
             store_carry(sl.carries, nruns - 1, 0);
         } else {
@@ -687,9 +691,13 @@ __device__ __forceinline__ void bulk_store(void* dst, const void* src, unsigned 
 }
 
 // tile_inner with the tile (and the partner's tile) brought in and written back
-// by bulk copies.  `bar` is an initialised barrier of this CTA (phase 0 unused).
-// If the load does not complete within the poll limit, the slot is flagged, the
-// copy is waited for once more, and the tile is left alone.
+// by bulk copies.  `bar` is a barrier of this CTA initialised for one arrival;
+// the load completes its phase 0, which is the phase waited on (parity 0).
+// If the load does not complete within the poll limit, the slot is flagged
+// SF_WAIT_TIMEOUT, the copy is waited for once more, and the tile is left
+// alone; if that second wait runs out too, SF_COPY_ABANDONED records that the
+// CTA left with the copy possibly still in flight.  Either flag makes the host
+// discard the step.
 template <int F, int G, int LASTP, int NT, class Sync>
 __device__ __forceinline__ void tile_inner_bulk(const Slot& sl, const Slot& pb, bool square, const PlanDev& pl,
                                                 int cta, int tid, double2* tile, double2* tile2,
@@ -703,7 +711,7 @@ __device__ __forceinline__ void tile_inner_bulk(const Slot& sl, const Slot& pb, 
     }
     if (!mbar_wait(bar, 0)) {
         if (tid == 0) atomicOr(&sl.st->flags, SF_WAIT_TIMEOUT);
-        mbar_wait(bar, 0);
+        if (!mbar_wait(bar, 0) && tid == 0) atomicOr(&sl.st->flags, SF_COPY_ABANDONED);
         return;
     }
     smem_fft_fwd<F, G, NT, true>(tile, pl.wF[LASTP], tid, sync);
@@ -906,6 +914,195 @@ __global__ void __launch_bounds__(2 * F0 * TPB) k_last(const Slot* __restrict__ 
         // the partner index is fixed by the host before the step: safe to read early
         tile_last<F0, 2 * F0 * TPB>(sl, slots[st->partner], pl, blockIdx.x, threadIdx.x, tile, cl, ch, BlockSync(),
                                     PdlActive{st, true});
+    }
+    pdl_trigger();
+}
+
+// ---------------------------------------------------------------------------
+// One residue, a chain of squarings: the last pass of squaring i and the first
+// pass of squaring i+1 in ONE kernel (k_edge), for the same column tile (RUN
+// columns x F0 rows), so the new digits go from the fold straight into the
+// carry fix-up and the weight, without a kernel boundary or a round trip
+// through global memory.  The only dependency between tiles is the run carry:
+// every carry entering this tile's runs comes from the tile before it in the
+// ring of tiles (tile c-1; for tile 0, the last tile, whose last run also feeds
+// the top-digit reduction).  So each CTA publishes its carries with a release
+// flag (the slot's step count) and waits, with a bounded number of polls, for
+// its predecessor's flag; a wait that runs out sets SF_WAIT_TIMEOUT and the CTA
+// skips its first-pass half, so the host discards the chunk.  All CTAs of the
+// launch are resident together (a few KB of shared memory each, and the next
+// kernel only starts once every CTA has passed its wait), so the wait ends.
+// The operations on every value are those of tile_last and tile_first, in the
+// same order: residues are bit-identical to the k_last + k_first sequence.
+// The top digit of the squaring being finished is read from tope[] (indexed by
+// the step parity) because tile 0 writes the next one while others may still
+// read it.
+
+constexpr int kEdgePolls = 1 << 22;
+
+__device__ __forceinline__ void flag_publish(long long* f, long long v) {
+    asm volatile("st.release.gpu.global.s64 [%0], %1;" ::"l"(f), "l"(v) : "memory");
+}
+__device__ __forceinline__ long long flag_read(const long long* f) {
+    long long v;
+    asm volatile("ld.acquire.gpu.global.s64 %0, [%1];" : "=l"(v) : "l"(f) : "memory");
+    return v;
+}
+// A carry written by another CTA of this launch (read past the L1 cache).
+__device__ __forceinline__ i128 load_carry_cg(const long long* c, long long idx) {
+    const unsigned long long lo = (unsigned long long)__ldcg(c + 2 * idx);
+    const long long hi = __ldcg(c + 2 * idx + 1);
+    return (i128)(((unsigned __int128)(unsigned long long)hi << 64) | lo);
+}
+
+template <int F0, int TPB = 1>
+__global__ void __launch_bounds__(2 * F0 * TPB) k_edge(const PlanDev pl, const Slot one, long long* __restrict__ eflags) {
+    constexpr int NT = 2 * F0 * TPB;
+    constexpr int G = RUN;
+    constexpr int PER = (F0 * G + NT - 1) / NT;
+    __shared__ double2 tile[F0 * RUN];
+    __shared__ long long cl[F0 * RUN];
+    __shared__ long long ch[F0 * RUN];
+    __shared__ int dsm[F0 * RUN];
+    __shared__ int go;
+    const Slot& sl = one;
+    SlotState* st = sl.st;
+    const int cta = blockIdx.x, tid = threadIdx.x;
+    const int S0 = pl.S[0];
+    const int r0 = cta * G;
+    const long long nruns = pl.M / RUN;
+    const double2* __restrict__ tw = pl.tw[0];
+    double2 ct[PER], cwi[PER], cwf[PER];  // constants, loaded before waiting on the previous kernel
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F0 * G) {
+            const int q = e / G, t = e % G;
+            ct[i] = tw[q * S0 + r0 + t];
+            cwi[i] = sl.wi[r0 + t + q * S0];
+            cwf[i] = sl.wf[r0 + t + q * S0];
+        }
+    }
+    pdl_wait();
+    // ---- squaring i: pass 0 inverse, unweight, round, Montgomery fold, in-run carry ----
+    const unsigned long long j0 = (unsigned long long)r0 + (unsigned long long)tid * S0;
+    const long long run = (long long)(j0 / RUN);
+    const long long step_ = st->step;  // squarings done, counting this one
+    int4 v0 = make_int4(0, 0, 0, 0), v1 = v0;
+    long long ta_ = 0;
+    if (tid < F0) {
+        const int4* dp = reinterpret_cast<const int4*>(sl.digits + j0);
+        v0 = dp[0];
+        v1 = dp[1];
+        ta_ = st->tope[step_ & 1];
+    }
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F0 * G) tile[e] = cmulc(sl.spec[r0 + e % G + (e / G) * S0], ct[i]);
+    }
+    __syncthreads();
+    smem_fft_inv<F0, G, NT, false>(tile, pl.wF[0], tid, BlockSync());
+    unsigned long long emax = 0;
+    int badr = 0;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F0 * G) {
+            const double2 z = cmul(tile[e], cwi[i]);
+            cl[e] = round_track(z.x, emax, badr);
+            ch[e] = round_track(z.y, emax, badr);
+        }
+    }
+    if (badr) {
+        emax = (unsigned long long)__double_as_longlong(1.0);
+        atomicOr(&st->flags, SF_ROUND_RANGE);
+    }
+    emax = warp_max_u64(emax);
+    if ((tid & 31) == 0 && emax > 0) atomicMax(&st->maxerr_bits, emax);
+    __syncthreads();
+    int nd[RUN] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (tid < F0) {
+        const int dv[RUN] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+        const i128 ta = (i128)ta_;
+        const i128 s = (i128)sched_mul(st, step_ - 1);
+        const i128 kk = (i128)sl.k;
+        if (run == 0) store_pend(st, s * ta * ta);
+        i128 carry = 0;
+#pragma unroll
+        for (int t = 0; t < RUN; ++t) {
+            const int e = tid * G + t;
+            const i128 u = s * ((i128)ch[e] + ta * (i128)dv[t] + ta * (i128)dv[t] - kk * (i128)cl[e]);
+            carry += u;
+            nd[t] = (int)take_digit(carry, digit_width(j0 + t, sl.n, pl.lgM));
+        }
+        store_carry(sl.carries, run, carry);
+    }
+    // ---- publish this tile's carries; wait for those of the tile before it ----
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        flag_publish(eflags + cta, step_);
+        const long long* pf = eflags + (cta == 0 ? (int)gridDim.x - 1 : cta - 1);
+        int ok = 0;
+        for (int i = 0; i < kEdgePolls; ++i) {
+            if (flag_read(pf) == step_) {
+                ok = 1;
+                break;
+            }
+        }
+        if (!ok) atomicOr(&st->flags, SF_WAIT_TIMEOUT);
+        go = ok;
+    }
+    __syncthreads();
+    if (!go) {
+        pdl_trigger();
+        return;
+    }
+    // ---- squaring i+1: carry fix-up, top reduction, weight, pass 0 forward ----
+    if (tid < F0) {
+        i128 cin;
+        if (run > 0) {
+            cin = load_carry_cg(sl.carries, run - 1);
+            store_carry(sl.carries, run - 1, 0);
+        } else {
+            const i128 tp = load_pend(st) + load_carry_cg(sl.carries, nruns - 1);
+            const i128 kk = (i128)sl.k;
+            const i128 q = floor_div(2 * tp + kk, 2 * kk);
+            const long long new_top = (long long)(tp - q * kk);
+            cin = -q;
+            st->top = new_top;
+            st->tope[(step_ + 1) & 1] = new_top;
+            store_pend(st, (i128)new_top);
+            store_carry(sl.carries, nruns - 1, 0);
+        }
+        int bad = 0;
+        fixup_run(nd, cin, j0, sl.n, pl.lgM, bad);
+        if (bad) atomicOr(&st->flags, SF_DIGIT_OVERFLOW);
+        int4* dp = reinterpret_cast<int4*>(sl.digits + j0);
+        dp[0] = make_int4(nd[0], nd[1], nd[2], nd[3]);
+        dp[1] = make_int4(nd[4], nd[5], nd[6], nd[7]);
+#pragma unroll
+        for (int t = 0; t < RUN; ++t) dsm[tid * G + t] = nd[t];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F0 * G) {
+            const double d = (double)dsm[e];
+            tile[e] = make_double2(d * cwf[i].x, d * cwf[i].y);
+        }
+    }
+    __syncthreads();
+    smem_fft_fwd<F0, G, NT, false>(tile, pl.wF[0], tid, BlockSync());
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F0 * G) {
+            const int p = e / G, t = e % G;
+            sl.spec[r0 + t + p * S0] = cmul(tile[e], ct[i]);
+        }
     }
     pdl_trigger();
 }

@@ -77,11 +77,14 @@ __device__ __forceinline__ uint32_t mpow2(uint32_t e, const Mont& M) {
 
 // Segment [lo, lo + 2*bits): bit b <-> odd number lo + 2b + 1.  Composite bits
 // are set by the base primes (q^2 <= number); zero bits are primes (except 1).
+// `live` (optional): the number of candidates still without a factor; at 0 the
+// launch has nothing to sieve for and returns at once.
 __global__ void __launch_bounds__(kSieveThreads) k_sieve(unsigned long long lo, const uint32_t* __restrict__ base,
                                                          int nbase, unsigned long long limit,
                                                          uint32_t* __restrict__ out, unsigned* __restrict__ count,
-                                                         unsigned cap) {
+                                                         unsigned cap, const uint32_t* __restrict__ live) {
     __shared__ uint32_t bits[kSubWords];
+    if (live && *live == 0u) return;
     const unsigned long long c_lo = lo + 2ull * kSubBits * blockIdx.x;  // even
     for (int w = threadIdx.x; w < kSubWords; w += blockDim.x) bits[w] = 0u;
     __syncthreads();
@@ -220,7 +223,7 @@ extern "C" int pg_prefilter(const uint64_t* ks, const uint32_t* ns, size_t count
         const unsigned long long limit = std::min<unsigned long long>(bound, lo + kSegNumbers);
         const int ctas = (int)((std::min<unsigned long long>(kSegNumbers, limit - lo) + 2ull * kSubBits - 1) /
                                (2ull * kSubBits));
-        k_sieve<<<ctas, kSieveThreads, 0, st>>>(lo, d_base, (int)base.size(), limit, d_primes, d_count, cap);
+        k_sieve<<<ctas, kSieveThreads, 0, st>>>(lo, d_base, (int)base.size(), limit, d_primes, d_count, cap, nullptr);
         ck(cudaGetLastError());
         unsigned np = 0;
         ck(cudaMemcpyAsync(&np, d_count, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
@@ -264,11 +267,12 @@ extern "C" int pg_prefilter(const uint64_t* ks, const uint32_t* ns, size_t count
 // file-scope device array of fixed size.  Every GPU on which this library is
 // loaded holds that array until the process exits.
 //
-// The kernels are the same sieve as pg_prefilter; the test kernel computes
-// 2^{n_i} mod p per candidate (the live list is not sorted by n, since sorting
-// would need the candidates on the host), and the live list is compacted on the
-// device, so one call is a fixed sequence of launches on the caller's stream
-// with no host synchronisation.
+// The kernels are the same sieve and the same test as pg_prefilter: the
+// candidates are ranked by n on the device once per call (so each prime walks
+// them with small exponent steps, as k_test does), and the live list is
+// compacted on the device in order, so one call is a fixed sequence of
+// launches on the caller's stream with no host synchronisation.  Once every
+// candidate has a factor, the remaining launches return at once.
 namespace pgpf {
 
 constexpr unsigned long long kNaSegNumbers = 1ull << 22;        // numbers per sieve launch
@@ -282,12 +286,31 @@ constexpr size_t kNaOffPrimes = kNaOffBase + kNaBaseCap;
 constexpr size_t kNaOffLive0 = kNaOffPrimes + kNaPrimeCap;
 constexpr size_t kNaOffLive1 = kNaOffLive0 + kNaMaxCount;
 constexpr size_t kNaWords = kNaOffLive1 + kNaMaxCount;
+constexpr int kNaRankThreads = 1024;
+constexpr int kNaCompactThreads = 1024;
 
-__global__ void k_na_seed(uint32_t* __restrict__ ctrl, uint32_t* __restrict__ live0, unsigned count,
-                          unsigned long long* __restrict__ factor) {
+// Live list 0 = all candidates ordered by (n, index): candidate i goes to its
+// rank, the number of candidates before it in that order (count^2 comparisons,
+// under a millisecond at the 65,536 cap).  Also clears the results and counters.
+__global__ void __launch_bounds__(kNaRankThreads) k_na_seed(const uint32_t* __restrict__ ns, unsigned count,
+                                                            uint32_t* __restrict__ ctrl, uint32_t* __restrict__ live0,
+                                                            unsigned long long* __restrict__ factor) {
+    __shared__ uint32_t tile[kNaRankThreads];
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t ni = i < count ? ns[i] : 0u;
+    unsigned rank = 0;
+    for (unsigned base = 0; base < count; base += kNaRankThreads) {
+        __syncthreads();
+        if (base + threadIdx.x < count) tile[threadIdx.x] = ns[base + threadIdx.x];
+        __syncthreads();
+        const unsigned m = min((unsigned)kNaRankThreads, count - base);
+        for (unsigned t = 0; t < m; ++t) {
+            const uint32_t nj = tile[t];
+            rank += (nj < ni || (nj == ni && base + t < i)) ? 1u : 0u;
+        }
+    }
     if (i < count) {
-        live0[i] = i;
+        live0[rank] = i;
         factor[i] = ~0ull;
     }
     if (i == 0) {
@@ -297,11 +320,14 @@ __global__ void k_na_seed(uint32_t* __restrict__ ctrl, uint32_t* __restrict__ li
     }
 }
 
-// One thread per prime of the segment, every live candidate.
+// One thread per prime of the segment, walking the live candidates in n order:
+// 2^{n_i} mod p advances by 2^{n_i - n_{i-1}} (the walk of k_test).
 __global__ void k_na_test(const uint32_t* __restrict__ primes, const uint32_t* __restrict__ nprimes,
                           const unsigned long long* __restrict__ ks, const uint32_t* __restrict__ ns,
                           const uint32_t* __restrict__ live, const uint32_t* __restrict__ nlive,
                           unsigned long long* __restrict__ factor) {
+    const unsigned nl = *nlive;
+    if (nl == 0u) return;
     const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned np = min(*nprimes, kNaPrimeCap);
     if (idx >= np) return;
@@ -309,22 +335,54 @@ __global__ void k_na_test(const uint32_t* __restrict__ primes, const uint32_t* _
     if (p < 3) return;
     const Mont M = make_mont(p);
     const uint32_t minus1 = p - 1;
-    const unsigned nl = *nlive;
+    uint32_t prev_n = 0;
+    uint32_t pw = mmul(1u, M.r2, M);  // 2^0 in Montgomery form
     for (unsigned j = 0; j < nl; ++j) {
         const uint32_t i = live[j];
+        const uint32_t n = ns[i];
+        pw = mmul(pw, mpow2(n - prev_n, M), M);
+        prev_n = n;
         const uint32_t km = (uint32_t)(ks[i] % p);
-        if (mmul(km, mpow2(ns[i], M), M) == minus1) atomicMin(&factor[i], (unsigned long long)p);
+        if (mmul(km, pw, M) == minus1) atomicMin(&factor[i], (unsigned long long)p);
     }
 }
 
-// Candidates still without a factor move to the other live list.
-__global__ void k_na_compact(const uint32_t* __restrict__ live, const uint32_t* __restrict__ nlive,
-                             const unsigned long long* __restrict__ factor, uint32_t* __restrict__ next,
-                             uint32_t* __restrict__ nnext) {
-    const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= *nlive) return;
-    const uint32_t i = live[j];
-    if (factor[i] == ~0ull) next[atomicAdd(nnext, 1u)] = i;
+// Candidates still without a factor move to the other live list, in order: one
+// CTA, each thread a contiguous share of the list, a block scan of the counts.
+__global__ void __launch_bounds__(kNaCompactThreads) k_na_compact(const uint32_t* __restrict__ live,
+                                                                  const uint32_t* __restrict__ nlive,
+                                                                  const unsigned long long* __restrict__ factor,
+                                                                  uint32_t* __restrict__ next,
+                                                                  uint32_t* __restrict__ nnext) {
+    __shared__ unsigned warp_sum[kNaCompactThreads / 32];
+    const unsigned nl = *nlive;
+    const unsigned t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const unsigned per = (nl + kNaCompactThreads - 1) / kNaCompactThreads;
+    const unsigned j0 = min(nl, t * per), j1 = min(nl, j0 + per);
+    unsigned mine = 0;
+    for (unsigned j = j0; j < j1; ++j) mine += factor[live[j]] == ~0ull ? 1u : 0u;
+    unsigned incl = mine;  // inclusive scan within the warp
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (unsigned)o) incl += v;
+    }
+    if (lane == 31) warp_sum[w] = incl;
+    __syncthreads();
+    if (w == 0) {  // scan of the warp totals
+        unsigned v = lane < kNaCompactThreads / 32 ? warp_sum[lane] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned u = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= (unsigned)o) v += u;
+        }
+        if (lane < kNaCompactThreads / 32) warp_sum[lane] = v;
+    }
+    __syncthreads();
+    unsigned pos = (w ? warp_sum[w - 1] : 0u) + incl - mine;
+    for (unsigned j = j0; j < j1; ++j) {
+        const uint32_t i = live[j];
+        if (factor[i] == ~0ull) next[pos++] = i;
+    }
+    if (t == kNaCompactThreads - 1) *nnext = pos;
 }
 
 __global__ void k_na_finish(unsigned long long* __restrict__ factor, unsigned count) {
@@ -394,17 +452,18 @@ extern "C" int pg_prefilter_noalloc(const uint64_t* d_ks, const uint32_t* d_ns, 
     unsigned long long* fac = reinterpret_cast<unsigned long long*>(d_smallest_factor);
     const unsigned cnt = (unsigned)count;
     const unsigned cblocks = (cnt + 255) / 256;
-    k_na_seed<<<cblocks, 256, 0, st>>>(ctrl, live[0], cnt, fac);
+    k_na_seed<<<(cnt + kNaRankThreads - 1) / kNaRankThreads, kNaRankThreads, 0, st>>>(d_ns, cnt, ctrl, live[0],
+                                                                                        fac);
     int cur = 0;
     for (unsigned long long lo = 0; lo < bound; lo += kNaSegNumbers) {
         if (cudaMemsetAsync(ctrl, 0, sizeof(uint32_t), st) != cudaSuccess) return PG_ECUDA;
         const unsigned long long limit = std::min<unsigned long long>(bound, lo + kNaSegNumbers);
         const int ctas = (int)((limit - lo + 2ull * kSubBits - 1) / (2ull * kSubBits));
         k_sieve<<<ctas, kSieveThreads, 0, st>>>(lo, s + kNaOffBase, (int)g_na_nbase, limit, primes, ctrl,
-                                                kNaPrimeCap);
+                                                kNaPrimeCap, ctrl + 1 + cur);
         k_na_test<<<kNaPrimeCap / 256, 256, 0, st>>>(primes, ctrl, ks, d_ns, live[cur], ctrl + 1 + cur, fac);
-        if (cudaMemsetAsync(ctrl + 1 + (cur ^ 1), 0, sizeof(uint32_t), st) != cudaSuccess) return PG_ECUDA;
-        k_na_compact<<<cblocks, 256, 0, st>>>(live[cur], ctrl + 1 + cur, fac, live[cur ^ 1], ctrl + 1 + (cur ^ 1));
+        k_na_compact<<<1, kNaCompactThreads, 0, st>>>(live[cur], ctrl + 1 + cur, fac, live[cur ^ 1],
+                                                      ctrl + 1 + (cur ^ 1));
         cur ^= 1;
     }
     k_na_finish<<<cblocks, 256, 0, st>>>(fac, cnt);

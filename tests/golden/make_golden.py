@@ -1,9 +1,11 @@
 """Generate tests/golden/golden.json from the reference itself and GMP.
 
-Run in the build container only (it needs the reference sources, an x86-64
-host for the reference's AVX-512 engine, and libgmp.so.10):
+Run where the reference sources, an x86-64 host for the reference's AVX-512
+engine and libgmp.so.10 are present (PROTH_REF_SRC names the reference's
+prothlogic4.2 directory):
 
-    python tests/golden/make_golden.py
+    PROTH_REF_SRC=<path to prothlogic4.2> python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --large-only    # GMP only: the n = 2^20 section
 
 Sources of truth, in order:
   * oracle/_ref/ref_harness  -- the UNMODIFIED reference engine (fft_engine.cpp,
@@ -83,6 +85,32 @@ def ref_test(k, n, L, cwd):
     return int(last[0]), int(last[1], 16), float(last[2])
 
 
+LARGE_BLOCKS = 200  # RES64 every 1,000 squarings up to 200,000: bench runs of up to 200 steps are checked
+
+
+def large_section():
+    """The n = 2^20 configuration: x0 = a, RES64 after every 1,000 squarings up
+    to LARGE_BLOCKS * 1,000 (GMP, with the Proth-form reduction)."""
+    k, n = workloads.large()
+    a = base_of(k, n)
+    chain = _gmp.square_chain_proth(a, LARGE_BLOCKS * 1000, k, n, every=1000)
+    print("large", k, n, a, flush=True)
+    return {"k": k, "n": n, "a": a, "x0": "a", "every": 1000,
+            "res64": [format(c & M64, "016x") for c in chain], "final_sha256": digest(chain[-1])}
+
+
+def update_large_only():
+    """Recompute only the large section of an existing golden.json (GMP only;
+    needs neither the reference sources nor an x86-64 host)."""
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.json")
+    with open(out) as f:
+        g = json.load(f)
+    g["large"] = large_section()
+    with open(out, "w") as f:
+        json.dump(g, f, indent=1)
+    print("wrote", out)
+
+
 def main():
     global REF
     REF = build_ref()
@@ -141,14 +169,8 @@ def main():
             g["known"].append({"k": k, "n": n, "L": L, "base": base_of(k, n), "verdict": v,
                                "res64": format(r, "016x"), "source": "Run test log"})
             print("known", k, n, v, flush=True)
-    # 5. the large single-candidate configuration: x0 = a, 10,000 squarings, RES64 every 1,000 (GMP)
-    k, n = workloads.large()
-    N = k * (1 << n) + 1
-    a = base_of(k, n)
-    chain = _gmp.square_chain(a, 10000, N, every=1000)
-    g["large"] = {"k": k, "n": n, "a": a, "x0": "a", "every": 1000,
-                  "res64": [format(c & M64, "016x") for c in chain], "final_sha256": digest(chain[-1])}
-    print("large", k, n, a, flush=True)
+    # 5. the large single-candidate configuration (GMP)
+    g["large"] = large_section()
     # 6. full tests from the batched configurations, GMP only
     for k, n in workloads.uniform(count=3) + [c for c in workloads.uneven(count=40) if c[1] < 40000][:6]:
         N = k * (1 << n) + 1
@@ -179,4 +201,7 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if "--large-only" in sys.argv:
+        update_large_only()
+    else:
+        main()

@@ -127,6 +127,43 @@ def test_gmp_full_tests_batched(pg, golden):
     b.close()
 
 
+def _config_sample(cands, count, seed):
+    """A seeded sample of a configuration: mostly candidates past the small-prime
+    gate, plus a few gated ones (answered at submission)."""
+    rng = random.Random(seed)
+    passing = [c for c in cands if not _gated(*c)]
+    gated = [c for c in cands if _gated(*c)]
+    return rng.sample(passing, count - 4) + rng.sample(gated, 4)
+
+
+def _gated(k, n):
+    from tests import _gmp
+    return any(k % p and pow(2, n, p) == (-pow(k, -1, p)) % p for p in _gmp.GATE_PRIMES)
+
+
+@pytest.mark.parametrize("config", ["uniform", "uneven"])
+def test_batch_config_sample_vs_gmp(pg, gmp, config):
+    """Per-candidate parity at configuration scale: a seeded 64-candidate sample of
+    the 4,096-candidate uniform workload (n = 65,536, k < 10^6) or of the
+    2,048-candidate uneven one (n log-uniform in [8,192, 262,144]) through one
+    Gerbicz-checked batch; every verdict, base and RES64 equals GMP's."""
+    from prothlogic_gb300 import workloads
+    cands = workloads.uniform(count=4096) if config == "uniform" else workloads.uneven(count=2048)
+    sample = _config_sample(cands, 64, seed=7 if config == "uniform" else 8)
+    want = gmp.proth_tests(sample)  # spawned processes, beside this process's CUDA context
+    b = pg.Batch(64)
+    for i, (k, n) in enumerate(sample):
+        b.submit(k, n, i)
+    b.run(0)
+    got = {r["tag"]: r for r in b.poll()}
+    b.close()
+    assert len(got) == len(sample)
+    for i, (k, n) in enumerate(sample):
+        r = got[i]
+        assert r["status"] == 0, (k, n, r)
+        assert (r["verdict"], r["base"], r["res64"]) == want[i], (k, n)
+
+
 def test_batch_equals_single(pg, oracle):
     rng = random.Random(17)
     cands = [(2 * rng.randrange(1, 5000) + 1, rng.randrange(2048, 9000)) for _ in range(60)]
@@ -291,6 +328,53 @@ def test_reference_api_shim_is_a_drop_in(pg, gmp, golden):
                              capture_output=True, text=True, check=True).stdout.split("\n")
         got = [ln.split()[1] for ln in out if ln.strip()]
         assert got == t["res64"][:steps], (t["k"], t["n"])
+
+
+def _drive(args, stdin=""):
+    import subprocess
+    from prothlogic_gb300 import build as b
+    return subprocess.run([b.COMPAT_DRIVER] + [str(a) for a in args], input=stdin, capture_output=True, text=True,
+                          check=True).stdout
+
+
+@pytest.mark.parametrize("k,n", [(9505, 32768), (843, 120002)])
+def test_reference_autotune_through_shim(pg, k, n):
+    """auto_tune_fft_len's probe (dcore.cpp:20-81: all-ones residue of (n+63)/64
+    limbs, one limb short of a residue mod N, 100 squarings) gets the engine's real
+    roundoff error through the shim and accepts its first length, as the
+    reference engine does at these n (Run test:31: 0.00195 at n = 120002)."""
+    out = _drive(["autotune", n, k]).split("\n")
+    probes = [ln.split() for ln in out if ln.startswith("PROBE")]
+    L = int([ln for ln in out if ln.startswith("L ")][0].split()[1])
+    first = 256
+    while n / first > 18.0:
+        first *= 2
+    assert len(probes) == 1 and int(probes[0][1]) == first == L
+    assert 0.0 < float(probes[0][2]) < 0.30
+
+
+def test_reference_loop_through_shim(pg, golden):
+    """The squaring loop of execute_proth_test_fft (proth_logic.cpp:442-552), one
+    fft_square_karatsuba per step on L/4 limbs at the autotuned L, through the
+    shim: verdicts and RES64 of the reference's own golden tests (n = 32,768,
+    2,049, 4,096; at n = 4,096 the L/4 limbs are one short of a residue mod N, so
+    the caller's copy is truncated as the reference engine truncates it) and of its
+    console log's known prime 843*2^120002+1 (a = 5, Run test:41)."""
+    cases = [t for t in golden["tests"] if not t["gated"] and t["base"]]  # n = 32768, 2049, 4096
+    cases += [t for t in golden["known"] if t["k"] == 843]
+    assert len(cases) == 4
+    for t in cases:
+        k, n = t["k"], t["n"]
+        L = 256
+        while n / L > 18.0:
+            L *= 2
+        x0 = pow(t["base"], k, _N(k, n))
+        res = _drive(["test", k, n, L], format(x0, "x")).split()
+        assert res[0] == "RESULT"
+        verdict, res64, steps, err = int(res[1]), res[2], int(res[3]), float(res[5])
+        assert steps == n - 1
+        assert (verdict, res64) == (t["verdict"], t["res64"]), (k, n)
+        assert err < 0.4
 
 
 def test_resume_from_reference_checkpoint(pg, golden, tmp_path):

@@ -164,3 +164,134 @@ def test_tune_set_rejects_shapes_that_are_not_compiled(pg):
     bad = {"lg": 12, "slots": 1, "passes": 2, "f0": 16, "f1": 256, "f2": 0, "g_mid": 2, "g_inner": 2, "tpb": 1}
     with pytest.raises(pg.ProthGpuError):
         pg.tune_set(pg.TUNE_ONE, bad)
+
+
+# k_resident instances (radices, CTAs per residue, threads per CTA) for lone residues
+RESIDENT_LONE = [(11, 16, 128, 16, 128), (11, 16, 128, 16, 64), (11, 32, 64, 8, 256), (11, 32, 64, 8, 128),
+                 (12, 32, 128, 16, 256), (12, 32, 128, 16, 128)]
+
+
+def _resident_shape(lg, f0, f1, cl, nt):
+    return {"lg": lg, "slots": 1, "passes": 2, "f0": f0, "f1": f1, "f2": 0, "g_mid": 2, "g_inner": 2,
+            "tpb": 1, "cluster": 0, "resident": cl, "resident_threads": nt}
+
+
+@pytest.mark.parametrize("lg,f0,f1,cl,nt", RESIDENT_LONE)
+def test_resident_lone_residue_exact(pg, gmp, lg, f0, f1, cl, nt):
+    """A lone residue held in the shared memory of a cluster of CTAs (k_resident):
+    exact after single squarings (one launch each), after a chain of 300 (one
+    launch), and through the a^k powering (small-multiplier schedule) and the
+    Gerbicz-checked chain whose products run on the per-pass kernels."""
+    k, n = (9505, 32768) if lg == 11 else (9505, 60000)
+    assert pg.pick_fft_len(k, n) == 1 << lg
+    pg.tune_set(pg.TUNE_ONE, _resident_shape(lg, f0, f1, cl, nt))
+    try:
+        N = k * (1 << n) + 1
+        x = random.Random(lg * 100 + cl + nt).randrange(N)
+        with pg.Engine(k, n, flags=pg.FLAG_NO_GERBICZ) as e:
+            e.set_residue(x)
+            for i in range(4):
+                e.square(1)
+                x = x * x % N
+                assert e.get_residue() == x, i
+            e.square(300)
+            assert e.get_residue() == gmp.square_chain_proth(x, 300, k, n, every=300)[0]
+        with pg.Engine(k, n) as e:
+            e.pow_small(3, k)
+            assert e.get_residue() == pow(3, k, N)
+            e.square(2500)
+            assert e.get_residue() == gmp.square_chain_proth(pow(3, k, N), 2500, k, n, every=2500)[0]
+            assert e.stats()["gerbicz_checks"] >= 1
+    finally:
+        pg.tune_clear()
+
+
+def test_resident_whole_test_matches_reference(pg):
+    """The reference's own golden test at n = 32,768 (k = 9,505, base 3) with its
+    squarings resident in a 16-CTA cluster: verdict and RES64 unchanged."""
+    with open(GOLDEN) as f:
+        t = [t for t in json.load(f)["tests"] if (t["k"], t["n"]) == (9505, 32768)][0]
+    pg.tune_set(pg.TUNE_ONE, _resident_shape(11, 16, 128, 16, 128))
+    try:
+        r = pg.proth_test(9505, 32768)
+        assert (r["verdict"], r["base"], format(r["res64"], "016x")) == (t["verdict"], t["base"], t["res64"])
+    finally:
+        pg.tune_clear()
+
+
+@pytest.mark.parametrize("nt", [256, 1024])
+def test_resident_batch_exact(pg, gmp, nt):
+    """Batch residues one CTA each (k_resident with clusters of one) at n = 65,536:
+    a seeded sample of the uniform workload to verdict, equal to GMP."""
+    from prothlogic_gb300 import workloads
+    pg.tune_set(pg.TUNE_MANY, {"lg": 12, "slots": 2, "passes": 2, "f0": 64, "f1": 64, "f2": 0, "g_mid": 2,
+                               "g_inner": 8, "tpb": 1, "cluster": 0, "resident": 1, "resident_threads": nt})
+    try:
+        rng = random.Random(nt)
+        cands = rng.sample(workloads.uniform(count=4096), 24)
+        want = gmp.proth_tests(cands)
+        b = pg.Batch(24)
+        for i, (k, n) in enumerate(cands):
+            b.submit(k, n, i)
+        b.run(0)
+        got = {r["tag"]: r for r in b.poll()}
+        b.close()
+        for i in range(len(cands)):
+            assert got[i]["status"] == 0
+            assert (got[i]["verdict"], got[i]["base"], got[i]["res64"]) == want[i], cands[i]
+    finally:
+        pg.tune_clear()
+
+
+@pytest.mark.parametrize("shape", [
+    {"passes": 3, "f0": 64, "f1": 32, "f2": 32, "g_mid": 2, "g_inner": 4, "tpb": 1, "cluster": 8},
+    {"passes": 3, "f0": 16, "f1": 64, "f2": 64, "g_mid": 2, "g_inner": 2, "tpb": 2, "cluster": 0},
+    {"passes": 3, "f0": 32, "f1": 64, "f2": 64, "g_mid": 2, "g_inner": 2, "tpb": 1, "cluster": 8, "tpb_outer": 2},
+])
+def test_edge_fused_chain_matches_large_configuration(pg, shape):
+    """n = 2^20 with the last pass of every squaring and the first pass of the next
+    in one kernel (k_edge, carry hand-over through release/acquire flags), the
+    Gerbicz check on (graph-replayed chains, the check chain on a second stream,
+    products on the plain kernels): RES64 after 1,000 and 2,000 squarings equal
+    the GMP values."""
+    with open(GOLDEN) as f:
+        g = json.load(f)["large"]
+    pg.tune_set(pg.TUNE_ONE, dict(shape, lg=16, slots=1, edge=1))
+    try:
+        with pg.Engine(g["k"], g["n"]) as e:
+            e.set_residue(g["a"])
+            for i in range(2):
+                e.square(g["every"])
+                assert format(e.get_residue() & M64, "016x") == g["res64"][i], i
+            assert e.stats()["gerbicz_failures"] == 0
+    finally:
+        pg.tune_clear()
+
+
+@pytest.mark.parametrize("lg,k,n,f0,f1,tpb", [(11, 9505, 32768, 32, 64, 4), (12, 77, 60000, 64, 64, 1),
+                                             (13, 3, 130000, 64, 128, 2)])
+def test_edge_fused_chain_steps_exact(pg, gmp, lg, k, n, f0, f1, tpb):
+    """Two-pass lengths with k_edge: exact after single squarings (a chain of one
+    has no fused pass), after chains of 7 and 130 (fused passes, graph replay and
+    a remainder), and across a rollback-free Gerbicz run."""
+    assert pg.pick_fft_len(k, n) == 1 << lg
+    pg.tune_set(pg.TUNE_ONE, {"lg": lg, "slots": 1, "passes": 2, "f0": f0, "f1": f1, "f2": 0, "g_mid": 2,
+                              "g_inner": 2, "tpb": tpb, "cluster": 0, "edge": 1})
+    try:
+        N = k * (1 << n) + 1
+        x = random.Random(lg).randrange(N)
+        with pg.Engine(k, n, flags=pg.FLAG_NO_GERBICZ) as e:
+            e.set_residue(x)
+            e.square(1)
+            x = x * x % N
+            assert e.get_residue() == x
+            for c in (7, 130):
+                e.square(c)
+                x = gmp.square_chain_proth(x, c, k, n, every=c)[0]
+                assert e.get_residue() == x, c
+        with pg.Engine(k, n) as e:
+            e.set_residue(x)
+            e.square(2300)
+            assert e.get_residue() == gmp.square_chain_proth(x, 2300, k, n, every=2300)[0]
+    finally:
+        pg.tune_clear()

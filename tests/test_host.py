@@ -165,3 +165,37 @@ def test_autotune_engine_rejects_unsupported_sizes():
     with pytest.raises(pg.ProthGpuError) as ei:
         pg.autotune_engine(3, 100)
     assert ei.value.status == pg.PG_EINVAL
+
+
+def test_reference_callers_link_against_the_gpu_shim(tmp_path):
+    """The reference's own callers (dcore.cpp, worker.cpp, pipeline_proth.cpp,
+    proth_logic.cpp, checkpoint_manager.cpp, storage_core.cpp, progress_core.cpp),
+    compiled unmodified, link against the shim and libprothgpu.so instead of the
+    reference engine (oracle/ref/build_ref_callers.sh).  Needs the reference
+    sources, named by PROTH_REF_SRC; nothing here runs them (no GPU)."""
+    import shutil
+    import subprocess
+    from oracle.build_oracle import ref_src
+    src = ref_src()
+    if not src or not os.path.isdir(src):
+        pytest.skip("reference sources not named (PROTH_REF_SRC)")
+    if not shutil.which("nm"):
+        pytest.skip("nm not available")
+    pg.load()  # libprothgpu.so built
+    here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    subprocess.run(["bash", os.path.join(here, "oracle", "ref", "build_ref_callers.sh"), src], check=True,
+                   capture_output=True)
+    binary = os.path.join(here, "oracle", "_ref", "ref_callers")
+    syms = subprocess.run(["nm", "-C", binary], capture_output=True, text=True, check=True).stdout
+    defined = {ln.split(" ", 2)[2].split("(")[0].split("[")[0] for ln in syms.splitlines() if " T " in ln}
+    undefined = {ln.split()[-1] for ln in syms.splitlines() if ln.strip().startswith("U ")}
+    # the reference's callers, and the engine entry points from the shim
+    for name in ["dispatch", "auto_tune_fft_len", "execute_proth_test_fft", "run_task_with_ctx",
+                 "build_proth_ff_tasks_for_range", "save_checkpoint", "load_checkpoint",
+                 "fft_init", "fft_destroy", "fft_square_karatsuba"]:
+        assert name in defined, name
+    # the squaring itself comes from libprothgpu.so
+    assert {"pg_create", "pg_square", "pg_peek_residue", "pg_set_residue", "pg_get_residue"} <= undefined
+    # and none of the reference engine's own code is linked in
+    for name in ["fft_stockham_radix8", "fft_bailey_2d", "unpack_karatsuba_overlap_add", "pack_karatsuba_limbs"]:
+        assert name not in syms, name

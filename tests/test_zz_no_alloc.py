@@ -1,5 +1,6 @@
 """pg_prefilter_noalloc (fixed device scratch, caller-owned device buffers)
-against pg_prefilter (the allocating entry point) on the same candidates.
+against pg_prefilter (the allocating entry point) and against the oracle's
+plain trial division (ora_smallest_factor) on the same candidates.
 
 Integer results, so the comparison is exact.  Two calls in a row share the one
 scratch array; the second must not see anything the first left behind."""
@@ -57,6 +58,7 @@ def _call(pg, torch, cands, bound):
 
 def test_noalloc_prefilter_matches_prefilter_two_calls(pg):
     torch = pytest.importorskip("torch")
+    from tests import _oracle
     calls = [
         (_random(31, 300) + _with_factor_above_segment(21, 40), 1 << 26),
         (_with_factor_above_segment(22, 40) + _random(32, 500) + [(3, 2048), (843, 120002)], 1 << 24),
@@ -68,8 +70,23 @@ def test_noalloc_prefilter_matches_prefilter_two_calls(pg):
         rc, got = _call(pg, torch, cands, bound)
         assert rc == 0, pg.load().pg_strerror(rc).decode()
         assert got == expected
+        assert got == [_oracle.lib().ora_smallest_factor(k, n, bound) for k, n in cands]
         results.append(got)
     assert results[1][-2:] == [19, 0]  # 19 | 3*2^2048+1; 843*2^120002+1 is prime
+
+
+def test_noalloc_prefilter_order_and_duplicates(pg):
+    """Candidates in any order of n, repeated ones, and a single candidate: the
+    device ranks them by n before the walk; answers stay those of trial division."""
+    torch = pytest.importorskip("torch")
+    from tests import _oracle
+    cands = _random(41, 50)
+    cands = cands[::-1] + cands[:7] + _with_factor_above_segment(23, 10)
+    bound = 1 << 24
+    for batch in (cands, cands[:1]):
+        rc, got = _call(pg, torch, batch, bound)
+        assert rc == 0
+        assert got == [_oracle.lib().ora_smallest_factor(k, n, bound) for k, n in batch]
 
 
 def test_noalloc_prefilter_rejects_more_than_its_scratch_holds(pg):
