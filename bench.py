@@ -406,104 +406,138 @@ def shim_sample(pg):
     return out
 
 
-def uneven_sample(pg, steps=200, warm=50, cpu_sq=60):
+def serving_sample(pg, rates=(16, 64, 256), window_s=15.0, drain_s=25.0):
+    """Configuration 5, short: Poisson arrivals (n log-uniform in [10,000, 300,000],
+    k odd < 10^5, seed 5) at each rate for `window_s` seconds, trial division by
+    every prime < 2^32 on its own stream, survivors through one Gerbicz-checked
+    batch under a 16 GiB budget; `drain_s` more seconds for the last verdicts."""
+    from prothlogic_gb300 import serve
+    rows = []
+    for lam in rates:
+        count = max(1, int(lam * window_s * 1.5))
+        arrivals = [(t, k, n) for t, k, n in workloads.serving(count, lam, seed=5) if t <= window_s]
+        _, sm = serve.serve(arrivals, time_limit=window_s + drain_s, window=window_s)
+        rows.append({"rate_per_s": lam, "arrived": sm["arrived"],
+                     "prefilter_rejected_frac": sm["prefilter_rejected"] / max(1, sm["completed"]),
+                     "tested": sm["tested"], "unfinished": sm["unfinished"], "p50_s": sm["p50_s"],
+                     "p99_s": sm["p99_s"], "p50_all_s": sm["p50_all_s"],
+                     "delivered_tests_per_hour": sm["delivered_tests_per_hour"],
+                     "offered_tests_per_hour": sm["offered_tests_per_hour"], "errors": sm["errors"]})
+    return {"workload": f"serving: Poisson arrivals for {window_s:.0f} s per rate, n log-uniform in "
+                        "[10000, 300000], k odd < 10^5 seed 5, pre-filter primes < 2^32",
+            "rows": rows,
+            "summary": {f"lambda={r['rate_per_s']}": [None if r["p50_s"] is None else round(r["p50_s"], 2),
+                                                       None if r["p99_s"] is None else round(r["p99_s"], 2),
+                                                       round(r["delivered_tests_per_hour"])] for r in rows},
+            "summary_columns": "p50 s, p99 s (arrival to verdict of tested candidates), delivered tests/hour"}
+
+
+def whole_batch(pg, cands, max_slots, parity_count=32, seed=11):
+    """Every candidate through one Gerbicz-checked batch to its verdict (wall
+    clock, submission to the last verdict), then a seeded subset of the tested
+    ones recomputed with GMP (processes spawned after the GPU work)."""
+    b = pg.Batch(max_slots)
+    t0 = time.perf_counter()
+    for i, (k, n) in enumerate(cands):
+        b.submit(k, n, i)
+    b.run(0)
+    wall = time.perf_counter() - t0
+    res = {r["tag"]: r for r in b.poll()}
+    b.close()
+    tested = [i for i, r in res.items() if r["base"]]
+    errors = sum(1 for r in res.values() if r["status"] != 0)
+    parity = "unchecked"
+    from tests import _gmp
+    if _gmp.available() and tested:
+        import random
+        pick = random.Random(seed).sample(tested, min(parity_count, len(tested)))
+        want = _gmp.proth_tests([cands[i] for i in pick])
+        bad = [cands[i] for i, w in zip(pick, want)
+               if (res[i]["verdict"], res[i]["base"], res[i]["res64"]) != w]
+        parity = (f"ok ({len(pick)} of {len(tested)} tested candidates equal GMP)" if not bad
+                  else f"MISMATCH at {bad[:4]}")
+    return {"verdicts": len(res), "tested": len(tested), "primes": sum(1 for r in res.values() if r["verdict"] == 1),
+            "errors": errors, "wall_s": wall, "tests_per_hour": len(tested) * 3600.0 / wall,
+            "gerbicz_checks": sum(r["gerbicz_checks"] for r in res.values()),
+            "gerbicz_failures": sum(r["gerbicz_failures"] for r in res.values()), "parity": parity}
+
+
+def one_at_a_time_us(pg, k, n, iters=500):
+    """Device-timed squarings of one candidate alone on the GPU (tuned one-residue shape)."""
+    e = pg.Engine(k, n, flags=pg.FLAG_NO_GERBICZ)
+    e.set_residue(3)
+    e.time_squarings(100)
+    ms, _ = e.time_squarings(iters)
+    e.close()
+    return ms * 1e3 / iters
+
+
+def uneven_sample(pg, cpu_sq=60):
     """Uneven batch: 2,048 candidates, n log-uniform in [8192, 262144], k odd < 10^5
-    (seed 4), every FFT-length class batched with its autotuned shape.  Per class:
-    device time per squaring step with all its candidates resident, and one
-    candidate alone; tests/hour = candidates / sum over them of (n-1+pow) x the
-    per-candidate cost of their class (classes run one after another)."""
-    cands = [(k, n) for k, n in workloads.uneven(count=2048) if not pg.gate_rejects(k, n)]
+    (seed 4), every FFT-length class with its autotuned shape, the whole workload
+    through one batch to the last verdict.  One at a time: per class, 500
+    squarings of one candidate alone, scaled to every member's chain."""
+    all_c = workloads.uneven(count=2048)
+    cands = [(k, n) for k, n in all_c if not pg.gate_rejects(k, n)]
     classes = {}
     for k, n in cands:
         classes.setdefault(pg.pick_fft_len(k, n).bit_length() - 1, []).append((k, n))
-    t_batch = t_one = 0.0
+    t_one = 0.0
     per_class = {}
     for lg, members in sorted(classes.items()):
-        tm = _chosen(pg.autotune(lg, slots=min(len(members), 1024), iters=50))
-        b = pg.Batch(len(members))
-        for i, (k, n) in enumerate(members):
-            b.submit(k, n, i)
-        b.run_timed(warm)
-        ms = b.run_timed(steps)
-        _, running, _ = b.pending()
-        b.close()
-        per_cand_sq = ms * 1e-3 / steps / max(1, running)
         to = _chosen(pg.autotune(lg, slots=1, iters=200))
-        k0, n0 = members[0]
-        e = pg.Engine(k0, n0, flags=pg.FLAG_NO_GERBICZ)
-        e.set_residue(3)
-        e.time_squarings(100)
-        ms1, _ = e.time_squarings(500)
-        e.close()
-        one_sq = ms1 * 1e-3 / 500
+        one_sq = one_at_a_time_us(pg, *members[0]) * 1e-6
         work = sum(n - 1 + max(0, k.bit_length() - 1) + GZ_EXTRA for k, n in members)
-        t_batch += work * per_cand_sq
         t_one += work * one_sq
-        per_class[f"2^{lg}"] = {"candidates": len(members), "running": running,
-                                "batch_us_per_candidate_squaring": per_cand_sq * 1e6,
-                                "one_at_a_time_us_per_squaring": one_sq * 1e6,
+        tm = _chosen(pg.autotune(lg, slots=min(len(members), 1024), iters=50))
+        per_class[f"2^{lg}"] = {"candidates": len(members), "one_at_a_time_us_per_squaring": one_sq * 1e6,
                                 "shape_batched": tm, "shape_one_at_a_time": to}
+    whole = whole_batch(pg, all_c, 2048)
     pg.tune_clear()
-    tph_batch = len(cands) * 3600.0 / t_batch
+    tph_batch = whole["tests_per_hour"]
     tph_one = len(cands) * 3600.0 / t_one
     cpu = cpu_tests_per_hour(cands, cpu_sq)
     return {"workload": "uneven: 2048 candidates, n log-uniform in [8192, 262144], k odd in [3,10^5) seed 4",
-            "tested": len(cands), "classes": per_class,
+            "tested": len(cands), "classes": per_class, "whole_run": whole, "parity": whole["parity"],
             "batched_tests_per_hour": tph_batch, "one_at_a_time_tests_per_hour": tph_one,
             "batched_over_one_at_a_time": tph_batch / tph_one,
             "cpu_reference_tests_per_hour": cpu["tests_per_hour"],
             "batched_over_cpu": tph_batch / cpu["tests_per_hour"], "cpu": cpu,
-            "sample": f"per class {steps} batch squaring steps after {warm} warm-up and 500 squarings of one "
-                      "candidate alone; tests/hour extrapolated to each candidate's full chain; "
-                      f"{len(cands)} of 2048 pass the reference's gate (the rest are composite at once)"}
+            "sample": "batched: the whole workload to its last verdict (wall clock); one at a time: 500 "
+                      "squarings of one candidate per class alone, scaled to each member's chain plus 1,500 "
+                      f"for its Gerbicz check; {len(cands)} of 2048 pass the reference's gate"}
 
 
-def batched_sample(pg, steps=300, warm=60):
+def batched_sample(pg):
     """Batched vs one-at-a-time tests/hour at n = 65536 (4096 candidates, k odd in
-    [3, 10^6), seed 3), from a bounded sample of squaring steps on the device."""
+    [3, 10^6), seed 3): the whole workload through one batch to the last verdict."""
     cands = workloads.uniform(count=4096)
     n = cands[0][1]
     lg = pg.pick_fft_len(cands[0][0], n).bit_length() - 1
     tuned_many = _chosen(pg.autotune(lg, slots=1024, iters=50))
     tuned_one = _chosen(pg.autotune(lg, slots=1, iters=200))
-    b = pg.Batch(4096)
-    admitted = 0
-    for i, (k, nn) in enumerate(cands):
-        b.submit(k, nn, i)
-    b.run_timed(warm)                       # admission + graph capture + warm-up
-    ms = b.run_timed(steps)
-    q, running, fin = b.pending()
-    admitted = running
-    b.close()
-    per_step_ms = ms / steps
+    whole = whole_batch(pg, cands, 4096)
     # n-1 squarings + the a^k powering (bitlen(k) - 1 <= 19) + the Gerbicz check at the
     # end of each chain: one block (1000) of the product chain and on average half a
     # block of tail recompute (the same allowance for the one-at-a-time engine)
     sq_per_test = n - 1 + 19 + GZ_EXTRA
-    tph_batch = admitted / (per_step_ms * 1e-3 * sq_per_test) * 3600.0
-    # one candidate at a time on the whole GPU (same engine, FFT length 4096)
-    k0 = cands[0][0]
-    e = pg.Engine(k0, n, flags=pg.FLAG_NO_GERBICZ)
-    e.set_residue(3)
-    e.time_squarings(200)
-    ms1, _ = e.time_squarings(2000)
-    e.close()
-    us1 = ms1 * 1e3 / 2000
+    us1 = one_at_a_time_us(pg, cands[0][0], n, iters=2000)
     tph_single = 3600.0 / (us1 * 1e-6 * sq_per_test)
     passing = [(k, nn) for k, nn in cands if not pg.gate_rejects(k, nn)]
     cpu = cpu_tests_per_hour(passing[: 4 * (os.cpu_count() or 1)], 200)
     pg.tune_clear()
+    tph_batch = whole["tests_per_hour"]
     return {"workload": "uniform: 4096 candidates, n=65536, k odd in [3,10^6) seed 3",
-            "running_slots": admitted, "batch_step_ms": per_step_ms,
+            "whole_run": whole, "parity": whole["parity"],
             "batched_tests_per_hour": tph_batch, "one_at_a_time_tests_per_hour": tph_single,
             "batched_over_one_at_a_time": tph_batch / tph_single,
             "one_at_a_time_us_per_squaring": us1,
             "shape_batched": tuned_many, "shape_one_at_a_time": tuned_one,
             "cpu_reference_tests_per_hour": cpu["tests_per_hour"],
             "batched_over_cpu": tph_batch / cpu["tests_per_hour"], "cpu": cpu,
-            "sample": f"{steps} batch squaring steps after {warm} warm-up; one-at-a-time 2000 squarings; "
-                      "tests/hour extrapolated to n-1+19 squarings per test plus 1,500 for the Gerbicz check "
-                      "(the CPU reference has none)"}
+            "sample": "batched: all 4,096 candidates to their last verdict (wall clock); one at a time: 2,000 "
+                      "squarings of one candidate alone scaled to n-1+19 squarings plus 1,500 for the Gerbicz "
+                      "check; CPU: the reference algorithm on all host cores, truncated tests scaled"}
 
 
 def run_gpu(args, world, rank, local, pgd):
@@ -615,6 +649,7 @@ def run_gpu(args, world, rank, local, pgd):
     uneven = uneven_sample(pg) if os.environ.get("PROTH_BENCH_UNEVEN", "1") == "1" else None
     single = single_sample(pg) if os.environ.get("PROTH_BENCH_SINGLE", "1") == "1" else None
     shim = shim_sample(pg) if os.environ.get("PROTH_BENCH_SHIM", "1") == "1" else None
+    serving = serving_sample(pg) if os.environ.get("PROTH_BENCH_SERVING", "1") == "1" else None
     cpu_ns, cpu_kind, cpu_used, cpu_L, cpu_fl = time_cpu_reference(k, n, cpu_sample_seconds())
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
@@ -655,6 +690,7 @@ def run_gpu(args, world, rank, local, pgd):
         "batched_uneven": uneven,
         "single_test": single,
         "reference_api_loop": shim,
+        "serving": serving,
     }
     line["results"] = compact_results(line)  # last key: the summary survives a truncated tail
     print(json.dumps(line), flush=True)
@@ -694,26 +730,17 @@ def compact_results(line):
 
 def uneven_full():
     """The whole uneven workload (2,048 candidates, every class, autotuned shapes)
-    through one batch to the last verdict; wall-clock tests/hour."""
+    through one batch to the last verdict; wall-clock tests/hour, a seeded subset
+    of the verdicts checked against GMP."""
     import prothlogic_gb300 as pg
     cands = workloads.uneven(count=2048)
     lgs = sorted({pg.pick_fft_len(k, n).bit_length() - 1 for k, n in cands})
     for lg in lgs:
         members = sum(1 for k, n in cands if pg.pick_fft_len(k, n).bit_length() - 1 == lg)
         pg.autotune(lg, slots=min(members, 1024), iters=50)
-    b = pg.Batch(2048)
-    t0 = time.perf_counter()
-    for i, (k, n) in enumerate(cands):
-        b.submit(k, n, i)
-    b.run(0)
-    wall = time.perf_counter() - t0
-    res = b.poll()
-    b.close()
-    tested = sum(1 for r in res if r["base"])
-    print(json.dumps({"workload": "uneven: 2048 candidates, n log-uniform in [8192, 262144], k odd in [3,10^5) seed 4",
-                      "verdicts": len(res), "tested": tested, "primes": sum(1 for r in res if r["verdict"] == 1),
-                      "errors": sum(1 for r in res if r["status"] != 0), "wall_s": wall,
-                      "tests_per_hour": tested * 3600.0 / wall, "classes": [f"2^{lg}" for lg in lgs]}))
+    whole = whole_batch(pg, cands, 2048)
+    print(json.dumps(dict(whole, workload="uneven: 2048 candidates, n log-uniform in [8192, 262144], "
+                                          "k odd in [3,10^5) seed 4", classes=[f"2^{lg}" for lg in lgs])))
     return 0
 
 

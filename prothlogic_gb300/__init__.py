@@ -14,7 +14,8 @@ import os
 from . import build as _build_mod
 
 __all__ = ["ProthGpuError", "Engine", "Batch", "proth_test", "execute_proth_test_fft",
-           "load", "pick_fft_len", "gate_rejects", "choose_base", "host_roundtrip", "prefilter"]
+           "load", "pick_fft_len", "gate_rejects", "choose_base", "host_roundtrip", "prefilter",
+           "PrefilterStream"]
 
 PG_OK = 0
 PG_EINVAL = 1
@@ -176,6 +177,74 @@ def prefilter(cands, bound=1 << 32):
     out = (_u64 * max(m, 1))()
     _check(load().pg_prefilter(ks, ns, m, bound, out), "pg_prefilter")
     return [int(out[i]) for i in range(m)]
+
+
+PREFILTER_NOALLOC_MAX_COUNT = 65536
+
+
+class PrefilterStream:
+    """pg_prefilter_noalloc queued on a CUDA stream of its own, so trial division
+    of newly arrived candidates runs on the GPU beside the batch instead of
+    between its slices.  The device and pinned host buffers are allocated once
+    here (torch provides them and the stream); each call copies the candidates
+    in, queues the pre-filter and the copy of its answers back, and returns at
+    once; poll() hands the answers over when the work has finished.  One call at
+    a time (the pre-filter's device scratch is shared by all calls)."""
+
+    def __init__(self, bound=1 << 32, cap=PREFILTER_NOALLOC_MAX_COUNT):
+        import torch
+        self._torch = torch
+        self.bound = int(bound)
+        self.cap = int(cap)
+        self.stream = torch.cuda.Stream()
+        self.h_k = torch.empty(self.cap, dtype=torch.int64, pin_memory=True)
+        self.h_n = torch.empty(self.cap, dtype=torch.int32, pin_memory=True)
+        self.h_f = torch.empty(self.cap, dtype=torch.int64, pin_memory=True)
+        self.d_k = torch.empty(self.cap, dtype=torch.int64, device="cuda")
+        self.d_n = torch.empty(self.cap, dtype=torch.int32, device="cuda")
+        self.d_f = torch.empty(self.cap, dtype=torch.int64, device="cuda")
+        self._count = None
+        self._event = None
+        # the first call on a device sets the scratch up, synchronously: do it now
+        self.start([(3, 2048)])
+        self._event.synchronize()
+        self.poll()
+
+    def busy(self):
+        return self._count is not None
+
+    def start(self, cands):
+        if self.busy():
+            raise ProthGpuError(9, "PrefilterStream.start: a call is still running")
+        m = len(cands)
+        if m > self.cap:
+            raise ProthGpuError(PG_ETOOBIG, f"PrefilterStream.start: {m} candidates (at most {self.cap})")
+        torch = self._torch
+        self.h_k[:m] = torch.tensor([k for k, _ in cands], dtype=torch.int64)
+        self.h_n[:m] = torch.tensor([n for _, n in cands], dtype=torch.int32)
+        with torch.cuda.stream(self.stream):
+            self.d_k[:m].copy_(self.h_k[:m], non_blocking=True)
+            self.d_n[:m].copy_(self.h_n[:m], non_blocking=True)
+            _check(load().pg_prefilter_noalloc(self.d_k.data_ptr(), self.d_n.data_ptr(), m, self.bound,
+                                               self.d_f.data_ptr(), self.stream.cuda_stream),
+                   "pg_prefilter_noalloc")
+            self.h_f[:m].copy_(self.d_f[:m], non_blocking=True)
+            self._event = torch.cuda.Event()
+            self._event.record(self.stream)
+        self._count = m
+
+    def poll(self):
+        """The smallest factors of the last call's candidates (0: none below the
+        bound) once it has finished, else None."""
+        if not self.busy() or not self._event.query():
+            return None
+        m, self._count = self._count, None
+        return [int(x) for x in self.h_f[:m].tolist()]
+
+    def close(self):
+        if self.busy():
+            self._event.synchronize()
+            self._count = None
 
 
 def slot_footprint(k, n):

@@ -85,9 +85,10 @@ __device__ __forceinline__ i128 res_carry(const long long* cout, unsigned rank, 
     return (i128)(((unsigned __int128)(unsigned long long)hi << 64) | (unsigned long long)lo);
 }
 
+// One CTA of a cluster per SM is what a lone residue needs; batch residues (CL = 1) want two per SM.
 template <int F0, int F1, int CL, int NT>
-__global__ void __launch_bounds__(NT) k_resident(const Slot* __restrict__ slots, int base, const PlanDev pl,
-                                                 long long steps) {
+__global__ void __launch_bounds__(NT, (CL == 1 && NT <= 512) ? 2 : 1)
+    k_resident(const Slot* __restrict__ slots, int base, const PlanDev pl, long long steps) {
     using R = ResGeom<F0, F1, CL, NT>;
     extern __shared__ __align__(16) unsigned char res_smem[];
     double2* A = reinterpret_cast<double2*>(res_smem);
@@ -110,6 +111,23 @@ __global__ void __launch_bounds__(NT) k_resident(const Slot* __restrict__ slots,
     const double2* __restrict__ tw = pl.tw[0];
     const double2* __restrict__ wf = sl.wf;
     const double2* __restrict__ wi = sl.wi;
+    // With few points per thread, the weights and twiddles a thread uses stay in
+    // registers for the whole chain instead of being read again every squaring.
+    constexpr bool CACHE = R::PER <= 2;
+    constexpr int NC = CACHE ? R::PER : 1;
+    double2 c_wf[NC], c_tf[NC], c_ti[NC], c_wi[NC];
+    if constexpr (CACHE) {
+#pragma unroll
+        for (int i = 0; i < R::PER; ++i) {
+            const int e = tid + i * NT, q = e / R::G0, t = e % R::G0;
+            const int j = (int)c * R::G0 + t + q * F1;
+            c_wf[i] = wf[j];
+            c_wi[i] = wi[j];
+            c_tf[i] = tw[q * F1 + (int)c * R::G0 + t];
+            const int g = e / F1, x = e % F1;
+            c_ti[i] = tw[((int)c * R::G1 + g) * F1 + x];
+        }
+    }
 
     // prologue: the CTA's digits and pending carries, the slot's top and pending top
     for (int lr = tid; lr < R::RUNS; lr += NT) {
@@ -174,7 +192,7 @@ __global__ void __launch_bounds__(NT) k_resident(const Slot* __restrict__ slots,
             const int e = tid + i * NT, q = e / R::G0, t = e % R::G0;
             const int j = (int)c * R::G0 + t + q * F1;
             const double d = (double)dig[(q * R::RPR + t / RUN) * RUN + t % RUN];
-            const double2 w = wf[j];
+            const double2 w = CACHE ? c_wf[i < NC ? i : 0] : wf[j];
             A[q * R::SA + t] = make_double2(d * w.x, d * w.y);
         }
         __syncthreads();
@@ -184,7 +202,7 @@ __global__ void __launch_bounds__(NT) k_resident(const Slot* __restrict__ slots,
         for (int i = 0; i < R::PER; ++i) {
             const int e = tid + i * NT, q = e / R::G0, t = e % R::G0;
             const int r = (int)c * R::G0 + t;
-            const double2 v = cmul(A[q * R::SA + t], tw[q * F1 + r]);
+            const double2 v = cmul(A[q * R::SA + t], CACHE ? c_tf[i < NC ? i : 0] : tw[q * F1 + r]);
             if constexpr (CL == 1) {
                 A[q * R::SA + t] = v;
             } else {
@@ -208,7 +226,7 @@ __global__ void __launch_bounds__(NT) k_resident(const Slot* __restrict__ slots,
         for (int i = 0; i < R::PER; ++i) {
             const int e = tid + i * NT, g = e / F1, x = e % F1;
             const int p = (int)c * R::G1 + g;
-            const double2 v = cmulc(B[g * R::SB + x], tw[p * F1 + x]);
+            const double2 v = cmulc(B[g * R::SB + x], CACHE ? c_ti[i < NC ? i : 0] : tw[p * F1 + x]);
             if constexpr (CL == 1) {
                 B[g * R::SB + x] = v;
             } else {
@@ -225,7 +243,7 @@ __global__ void __launch_bounds__(NT) k_resident(const Slot* __restrict__ slots,
             for (int i = 0; i < R::PER; ++i) {
                 const int e = tid + i * NT, q = e / R::G0, t = e % R::G0;
                 const int j = (int)c * R::G0 + t + q * F1;
-                const double2 z = cmul(A[q * R::SA + t], wi[j]);
+                const double2 z = cmul(A[q * R::SA + t], CACHE ? c_wi[i < NC ? i : 0] : wi[j]);
                 long long* cell = reinterpret_cast<long long*>(A + q * R::SA + t);
                 cell[0] = round_track(z.x, emax, badr);
                 cell[1] = round_track(z.y, emax, badr);

@@ -2,12 +2,14 @@
 
 Candidates arrive over time (seeded Poisson arrivals; n log-uniform in
 [10000, 300000], k odd in [3, 10^5)).  On arrival they are trial-divided on the
-GPU by every prime below 2^32 (pg_prefilter); survivors are submitted to the
-batched engine (pg_batch), which admits them under an HBM budget (the
-per-candidate device footprint of their FFT length), keeps residues and their
-checkpoints (every 10,000 squarings) on the device, and returns verdicts.
-Reported: p50/p99 time-to-verdict (arrival to verdict) and tests/hour, swept
-over arrival rates until throughput stops growing.
+GPU by every prime below 2^32 (pg_prefilter_noalloc, queued on a stream of its
+own beside the batch, so the division overlaps the squaring work instead of
+pausing it); survivors are submitted to the batched engine (pg_batch), which
+admits them under an HBM budget (the per-candidate device footprint of their
+FFT length), keeps residues and their checkpoints (every 10,000 squarings) on
+the device, and returns verdicts.  Reported: p50/p99 time-to-verdict (arrival to
+verdict) and tests/hour, swept over arrival rates until throughput stops
+growing.
 
     python -m prothlogic_gb300.serve --rates 16,32,64,128,256,512 --window 40
 """
@@ -16,7 +18,7 @@ import json
 import statistics
 import time
 
-from . import Batch, prefilter, slot_footprint, workloads
+from . import Batch, PrefilterStream, slot_footprint, workloads
 
 
 def _pct(xs, q):
@@ -32,30 +34,32 @@ def serve(arrivals, budget_bytes=16 << 30, max_slots=1024, prefilter_bound=1 << 
     """Run the loop over `arrivals` [(t_arrive_s, k, n)] (sorted by time).
 
     Returns per-candidate records and a summary.  Wall-clock times are host
-    times since the start of the run (the loop is synchronous with the GPU at
-    each slice).  `window`: the arrival window in seconds (default: the last
-    arrival); delivered throughput is counted over its second half, where the
-    loop is in its steady state, and candidates still running at `time_limit`
-    count as not delivered."""
+    times since the start of the run.  Arrivals wait for the pre-filter stream
+    (one call in flight, every candidate that arrived meanwhile in the next
+    call); the batch advances `slice_steps` squarings per loop turn while the
+    pre-filter works.  `window`: the arrival window in seconds (default: the
+    last arrival); delivered throughput is counted over its second half, where
+    the loop is in its steady state, and candidates still running at
+    `time_limit` count as not delivered."""
     b = Batch(max_slots)
     b.set_budget(budget_bytes)
+    pf = PrefilterStream(bound=prefilter_bound)
     t0 = time.perf_counter()
     i = 0
     meta = {}
     records = []
+    waiting = []    # arrived, not yet handed to the pre-filter
+    inflight = []   # in the pre-filter call now running
     busy_s = 0.0
     while True:
         now = time.perf_counter() - t0
-        due = []
         while i < len(arrivals) and arrivals[i][0] <= now:
-            due.append(arrivals[i])
+            waiting.append(arrivals[i])
             i += 1
-        if due:
-            t_pf = time.perf_counter()
-            factors = prefilter([(k, n) for _, k, n in due], bound=prefilter_bound)
+        factors = pf.poll()
+        if factors is not None:
             done_t = time.perf_counter() - t0
-            busy_s += time.perf_counter() - t_pf
-            for (ta, k, n), f in zip(due, factors):
+            for (ta, k, n), f in zip(inflight, factors):
                 if f:
                     records.append({"k": k, "n": n, "t_arrive": ta, "t_verdict": done_t, "verdict": 0,
                                     "factor": f, "tested": False})
@@ -63,6 +67,10 @@ def serve(arrivals, budget_bytes=16 << 30, max_slots=1024, prefilter_bound=1 << 
                     tag = len(meta)
                     meta[tag] = (ta, k, n)
                     b.submit(k, n, tag)
+            inflight = []
+        if waiting and not pf.busy():
+            inflight, waiting = waiting[:pf.cap], waiting[pf.cap:]
+            pf.start([(k, n) for _, k, n in inflight])
         q, r, f = b.pending()
         if q + r + f > 0:
             t_run = time.perf_counter()
@@ -74,13 +82,16 @@ def serve(arrivals, budget_bytes=16 << 30, max_slots=1024, prefilter_bound=1 << 
                 records.append({"k": k, "n": n, "t_arrive": ta, "t_verdict": t_now, "verdict": res["verdict"],
                                 "res64": res["res64"], "fft_len": res["fft_len"], "status": res["status"],
                                 "bumps": res["fft_bumps"], "tested": True})
+        elif pf.busy():
+            time.sleep(0.001)
         elif i < len(arrivals):
             time.sleep(max(0.0, min(0.5, arrivals[i][0] - (time.perf_counter() - t0))))
-        else:
+        elif not waiting:
             break
         if time_limit is not None and time.perf_counter() - t0 > time_limit:
             break
     wall = time.perf_counter() - t0
+    pf.close()
     b.close()
     tested = [r for r in records if r["tested"]]
     lat = [r["t_verdict"] - r["t_arrive"] for r in tested]

@@ -246,7 +246,7 @@ def test_resident_batch_exact(pg, gmp, nt):
 @pytest.mark.parametrize("shape", [
     {"passes": 3, "f0": 64, "f1": 32, "f2": 32, "g_mid": 2, "g_inner": 4, "tpb": 1, "cluster": 8},
     {"passes": 3, "f0": 16, "f1": 64, "f2": 64, "g_mid": 2, "g_inner": 2, "tpb": 2, "cluster": 0},
-    {"passes": 3, "f0": 32, "f1": 64, "f2": 64, "g_mid": 2, "g_inner": 2, "tpb": 1, "cluster": 8, "tpb_outer": 2},
+    {"passes": 3, "f0": 16, "f1": 64, "f2": 64, "g_mid": 2, "g_inner": 2, "tpb": 1, "cluster": 8, "tpb_outer": 2},
 ])
 def test_edge_fused_chain_matches_large_configuration(pg, shape):
     """n = 2^20 with the last pass of every squaring and the first pass of the next
