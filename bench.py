@@ -406,7 +406,7 @@ def shim_sample(pg):
     return out
 
 
-def serving_sample(pg, rates=(16, 64, 256), window_s=15.0, drain_s=25.0):
+def serving_sample(pg, rates=(16, 64, 256), window_s=20.0, drain_s=20.0):
     """Configuration 5, short: Poisson arrivals (n log-uniform in [10,000, 300,000],
     k odd < 10^5, seed 5) at each rate for `window_s` seconds, trial division by
     every prime < 2^32 on its own stream, survivors through one Gerbicz-checked
@@ -422,14 +422,18 @@ def serving_sample(pg, rates=(16, 64, 256), window_s=15.0, drain_s=25.0):
                      "tested": sm["tested"], "unfinished": sm["unfinished"], "p50_s": sm["p50_s"],
                      "p99_s": sm["p99_s"], "p50_all_s": sm["p50_all_s"],
                      "delivered_tests_per_hour": sm["delivered_tests_per_hour"],
+                     "completed_tests_per_hour": sm["tests_per_hour"],
                      "offered_tests_per_hour": sm["offered_tests_per_hour"], "errors": sm["errors"]})
     return {"workload": f"serving: Poisson arrivals for {window_s:.0f} s per rate, n log-uniform in "
                         "[10000, 300000], k odd < 10^5 seed 5, pre-filter primes < 2^32",
             "rows": rows,
             "summary": {f"lambda={r['rate_per_s']}": [None if r["p50_s"] is None else round(r["p50_s"], 2),
                                                        None if r["p99_s"] is None else round(r["p99_s"], 2),
-                                                       round(r["delivered_tests_per_hour"])] for r in rows},
-            "summary_columns": "p50 s, p99 s (arrival to verdict of tested candidates), delivered tests/hour"}
+                                                       round(r["completed_tests_per_hour"]),
+                                                       round(r["offered_tests_per_hour"])] for r in rows},
+            "summary_columns": "p50 s, p99 s (arrival to verdict of tested candidates), tests/hour completed "
+                               "(tests finished / time of the last verdict), offered (survivors of the "
+                               "pre-filter per hour of arrivals); the full-length sweep is the serve module's CLI"}
 
 
 def whole_batch(pg, cands, max_slots, parity_count=32, seed=11):
@@ -772,17 +776,19 @@ def parse_shape(spec, lg):
     return shape
 
 
-def ncu_target(shape=None):
-    """Small profiling target: one n = 1,048,576 residue, 200 squarings, no
-    Gerbicz; `shape` (see parse_shape) pins the launch shape."""
+def ncu_target(shape=None, k=None, n=None, squarings=200):
+    """Small profiling target: one residue (default the n = 1,048,576
+    configuration), `squarings` squarings, no Gerbicz; `shape` (see
+    parse_shape) pins the launch shape."""
     import prothlogic_gb300 as pg
-    k, n = workloads.large()
+    if k is None or n is None:
+        k, n = workloads.large()
     if shape:
         lg = pg.pick_fft_len(k, n).bit_length() - 1
         pg.tune_set(pg.TUNE_ONE, parse_shape(shape, lg))
     e = pg.Engine(k, n, flags=pg.FLAG_NO_GERBICZ)
     e.set_residue(5)
-    e.square(200)
+    e.square(squarings)
     print("res64 %016x" % (e.get_residue() & ((1 << 64) - 1)))
     e.close()
     return 0
@@ -796,11 +802,14 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ncu-target", action="store_true", help="run only the small profiling target")
     ap.add_argument("--shape", default=None, help="launch shape of the profiling target, e.g. 64x32x32,gi=4,cl=8")
+    ap.add_argument("--k", type=int, default=None, help="profiling target: k (with --n)")
+    ap.add_argument("--n", type=int, default=None, help="profiling target: n (with --k)")
+    ap.add_argument("--squarings", type=int, default=200, help="profiling target: squarings")
     ap.add_argument("--uneven-full", action="store_true", help="run the whole uneven batch to completion")
     ap.add_argument("--ncu-batch-target", action="store_true", help="run only the small batched profiling target")
     args = ap.parse_args()
     if args.ncu_target:
-        return ncu_target(args.shape)
+        return ncu_target(args.shape, args.k, args.n, args.squarings)
     if args.ncu_batch_target:
         return ncu_batch_target()
     if args.uneven_full:
