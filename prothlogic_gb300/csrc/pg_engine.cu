@@ -392,11 +392,16 @@ struct ResInst {
 };
 #define PG_RES(A, B, C, T) {A, B, C, T, k_resident<A, B, C, T>, ResGeom<A, B, C, T>::SMEM},
 static const ResInst kResInst[] = {
-    // one residue per cluster of 4..16 CTAs (lone residues)
+    // one residue per cluster of 4..16 CTAs (lone residues), 2^9 .. 2^14 points
+    PG_RES(16, 32, 4, 128) PG_RES(32, 32, 4, 256) PG_RES(32, 32, 4, 128) PG_RES(16, 64, 8, 128)
     PG_RES(16, 128, 16, 128) PG_RES(16, 128, 16, 64) PG_RES(32, 64, 8, 256) PG_RES(32, 64, 8, 128)
     PG_RES(32, 128, 16, 256) PG_RES(32, 128, 16, 128)
-    // one residue per CTA (batches)
+    PG_RES(64, 128, 16, 512) PG_RES(64, 128, 16, 256)
+    PG_RES(128, 128, 16, 1024) PG_RES(128, 128, 16, 512) PG_RES(128, 128, 16, 256)
+    // batch residues: one CTA each up to 2^12 points, two or four CTAs at 2^13, 2^14
+    PG_RES(16, 32, 1, 128) PG_RES(32, 32, 1, 256) PG_RES(32, 64, 1, 256) PG_RES(32, 64, 1, 512)
     PG_RES(64, 64, 1, 256) PG_RES(64, 64, 1, 1024)
+    PG_RES(64, 128, 2, 512) PG_RES(64, 128, 2, 1024) PG_RES(128, 128, 4, 512) PG_RES(128, 128, 4, 1024)
 };
 #undef PG_RES
 

@@ -409,10 +409,55 @@ __device__ __forceinline__ long long take_digit(i128& v, int b) {
     return lo;
 }
 
-__device__ __forceinline__ i128 floor_div(i128 a, i128 b) {  // b > 0
+// floor(a / b), b > 0.  Operands that fit in 63 bits (every k below 2^40 with the
+// usual top digits) take the 64-bit division, much cheaper than the 128-bit one
+// on the critical path of the top-digit reduction; the quotient is the same.
+__device__ __forceinline__ i128 floor_div(i128 a, i128 b) {
+    const i128 lim = (i128)1 << 62;
+    if (a > -lim && a < lim && b < lim) {
+        const long long a64 = (long long)a, b64 = (long long)b;
+        long long q = a64 / b64;
+        if ((a64 % b64) != 0 && a64 < 0) q -= 1;
+        return (i128)q;
+    }
     i128 q = a / b;
     if ((a % b) != 0 && a < 0) q -= 1;
     return q;
+}
+
+// a * b exactly, from one 64 x 64 -> 128-bit product (a and b signed).
+__device__ __forceinline__ i128 mul_wide(long long a, long long b) {
+    const unsigned long long lo = (unsigned long long)a * (unsigned long long)b;
+    const long long hi = __mul64hi(a, b);
+    return (i128)(((unsigned __int128)(unsigned long long)hi << 64) | lo);
+}
+
+// The Montgomery fold of one digit position of X_a X_b:  u_j = s (c_{M+j} +
+// top_a d^b_j + top_b d^a_j - k c_j)  (X_a X_b 2^-n = H - k Lo, the cross terms
+// of the top digits at weight 2^n).  Exact integer arithmetic.
+__device__ __forceinline__ i128 fold_term(long long cl, long long ch, int dv, int dw, long long ta, long long tb,
+                                          long long k, int s) {
+    const i128 x = (i128)ch + mul_wide(ta, dw) + mul_wide(tb, dv) - mul_wide(k, cl);
+    return s == 1 ? x : x * (i128)s;
+}
+
+// The in-run carry of one run of RUN digits starting at digit j0: u[t] are the
+// fold terms; writes the balanced digits nd[] and returns the carry out.  Digit
+// widths follow from S_j = ceil(j n / M), advanced by one add per digit.
+__device__ __forceinline__ i128 run_carry(const i128 (&u)[RUN], unsigned long long j0, unsigned n, int lgM,
+                                          int (&nd)[RUN]) {
+    unsigned long long acc = j0 * n + ((1ull << lgM) - 1);
+    unsigned long long p0 = acc >> lgM;
+    i128 carry = 0;
+#pragma unroll
+    for (int t = 0; t < RUN; ++t) {
+        acc += n;
+        const unsigned long long p1 = acc >> lgM;
+        carry += u[t];
+        nd[t] = (int)take_digit(carry, (int)(p1 - p0));
+        p0 = p1;
+    }
+    return carry;
 }
 
 __device__ __forceinline__ i128 load_pend(const SlotState* st) {
@@ -444,12 +489,17 @@ __device__ __forceinline__ i128 run_carry_in(const Slot& sl, long long run, long
 // is added there unnormalised, so the run's own carry-out stays valid.
 __device__ __forceinline__ void fixup_run(int (&dv)[RUN], i128 c, unsigned long long j0, unsigned n,
                                           int lgM, int& bad) {
+    unsigned long long acc = j0 * n + ((1ull << lgM) - 1);  // S_j = ceil(j n / M), one add per digit
+    unsigned long long p0 = acc >> lgM;
 #pragma unroll
     for (int t = 0; t < RUN; ++t) {
+        acc += n;
+        const unsigned long long p1 = acc >> lgM;
+        const int b = (int)(p1 - p0);
+        p0 = p1;
         if (c != 0) {
             i128 v = (i128)dv[t] + c;
             if (t < RUN - 1) {
-                const int b = digit_width(j0 + t, n, lgM);
                 dv[t] = (int)take_digit(v, b);
                 c = v;
             } else {
@@ -755,21 +805,21 @@ __device__ __forceinline__ void tile_last(const Slot& sl, const Slot& pb, const 
         }
     }
     if (!pre()) return;
-    // integer operands of the fold, loaded now so their latency overlaps the transform
+    // integer operands of the fold (the digits of both factors at this thread's
+    // points), loaded now so their latency overlaps the transform
     const unsigned long long j0 = (unsigned long long)r0 + (unsigned long long)tid * S0;
-    int4 v0 = make_int4(0, 0, 0, 0), v1 = v0, w0 = v0, w1 = v0;
-    long long ta_ = 0, tb_ = 0, step_ = 0;
-    if (tid < F0) {
-        const int4* dp = reinterpret_cast<const int4*>(sl.digits + j0);
-        const int4* qp = reinterpret_cast<const int4*>(pb.digits + j0);
-        v0 = dp[0];
-        v1 = dp[1];
-        w0 = qp[0];
-        w1 = qp[1];
-        ta_ = st->top;
-        tb_ = pb.st->top;
-        step_ = st->step;
+    int dvi[PER], dwi[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        dvi[i] = dwi[i] = 0;
+        if (e < F0 * G) {
+            const int j = r0 + e % G + (e / G) * S0;
+            dvi[i] = sl.digits[j];
+            dwi[i] = pb.digits[j];
+        }
     }
+    const long long ta_ = st->top, tb_ = pb.st->top, step_ = st->step;
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
         const int e = tid + i * NT;
@@ -794,25 +844,30 @@ __device__ __forceinline__ void tile_last(const Slot& sl, const Slot& pb, const 
     }
     emax = warp_max_u64(emax);
     if ((tid & 31) == 0 && emax > 0) atomicMax(&st->maxerr_bits, emax);
+    // the fold term of every point, by the thread that rounded it (in place of its two halves)
+    const int s_ = sched_mul(st, step_ - 1);
+    const long long k_ = (long long)sl.k;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int e = tid + i * NT;
+        if (e < F0 * G) {
+            const i128 u = fold_term(cl[e], ch[e], dvi[i], dwi[i], ta_, tb_, k_, s_);
+            cl[e] = (long long)(unsigned long long)u;
+            ch[e] = (long long)(u >> 64);
+        }
+    }
     sync();
     if (tid < F0) {
         const long long run = (long long)(j0 / RUN);
-        const int dv[RUN] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
-        const int dw[RUN] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
-        const i128 ta = (i128)ta_, tb = (i128)tb_;
-        const i128 s = (i128)sched_mul(st, step_ - 1);
-        const i128 kk = (i128)sl.k;
-        if (run == 0) store_pend(st, s * ta * tb);
-        i128 carry = 0;
-        int nd[RUN];
+        if (run == 0) store_pend(st, (i128)s_ * (i128)ta_ * (i128)tb_);
+        i128 u[RUN];
 #pragma unroll
         for (int t = 0; t < RUN; ++t) {
             const int e = tid * G + t;
-            // X_a X_b 2^-n = H - k Lo; cross terms top_a X_b + top_b X_a sit at weight 2^n
-            const i128 u = s * ((i128)ch[e] + ta * (i128)dw[t] + tb * (i128)dv[t] - kk * (i128)cl[e]);
-            carry += u;
-            nd[t] = (int)take_digit(carry, digit_width(j0 + t, sl.n, pl.lgM));
+            u[t] = (i128)(((unsigned __int128)(unsigned long long)ch[e] << 64) | (unsigned long long)cl[e]);
         }
+        int nd[RUN];
+        const i128 carry = run_carry(u, j0, sl.n, pl.lgM, nd);
         int4* dp = reinterpret_cast<int4*>(sl.digits + j0);
         dp[0] = make_int4(nd[0], nd[1], nd[2], nd[3]);
         dp[1] = make_int4(nd[4], nd[5], nd[6], nd[7]);
@@ -1024,19 +1079,15 @@ __global__ void __launch_bounds__(2 * F0 * TPB) k_edge(const PlanDev pl, const S
     int nd[RUN] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (tid < F0) {
         const int dv[RUN] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
-        const i128 ta = (i128)ta_;
-        const i128 s = (i128)sched_mul(st, step_ - 1);
-        const i128 kk = (i128)sl.k;
-        if (run == 0) store_pend(st, s * ta * ta);
-        i128 carry = 0;
+        const int s_ = sched_mul(st, step_ - 1);
+        if (run == 0) store_pend(st, (i128)s_ * (i128)ta_ * (i128)ta_);
+        i128 u[RUN];
 #pragma unroll
         for (int t = 0; t < RUN; ++t) {
             const int e = tid * G + t;
-            const i128 u = s * ((i128)ch[e] + ta * (i128)dv[t] + ta * (i128)dv[t] - kk * (i128)cl[e]);
-            carry += u;
-            nd[t] = (int)take_digit(carry, digit_width(j0 + t, sl.n, pl.lgM));
+            u[t] = fold_term(cl[e], ch[e], dv[t], dv[t], ta_, ta_, (long long)sl.k, s_);
         }
-        store_carry(sl.carries, run, carry);
+        store_carry(sl.carries, run, run_carry(u, j0, sl.n, pl.lgM, nd));
     }
     // ---- publish this tile's carries; wait for those of the tile before it ----
     __syncthreads();

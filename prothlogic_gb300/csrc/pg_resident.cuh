@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(NT, (CL == 1 && NT <= 512) ? 2 : 1)
     const int kbits = st->kbits, mul = st->mul;
     const unsigned n = sl.n;
     const int lgM = pl.lgM;
-    const i128 kk = (i128)sl.k;
+    const i128 kk = (i128)sl.k;  // the top-digit reduction
     const double2* __restrict__ tw = pl.tw[0];
     const double2* __restrict__ wf = sl.wf;
     const double2* __restrict__ wi = sl.wi;
@@ -235,24 +235,9 @@ __global__ void __launch_bounds__(NT, (CL == 1 && NT <= 512) ? 2 : 1)
             }
         }
         res_sync<CL>();
-        // 6. pass 0 inverse; unweight and round in place (the two int64 halves of the product)
+        // 6. pass 0 inverse; unweight, round, and the fold term of every point, in place:
+        //    u_j = s (c_{M+j} + 2 top d_j - k c_j)  (X^2 2^-n = H - k Lo, cross terms at weight 2^n)
         smem_fft_inv<F0, R::G0, NT, false, R::SA>(A, pl.wF[0], tid, BlockSync());
-        {
-            int badr = 0;
-#pragma unroll 4
-            for (int i = 0; i < R::PER; ++i) {
-                const int e = tid + i * NT, q = e / R::G0, t = e % R::G0;
-                const int j = (int)c * R::G0 + t + q * F1;
-                const double2 z = cmul(A[q * R::SA + t], CACHE ? c_wi[i < NC ? i : 0] : wi[j]);
-                long long* cell = reinterpret_cast<long long*>(A + q * R::SA + t);
-                cell[0] = round_track(z.x, emax, badr);
-                cell[1] = round_track(z.y, emax, badr);
-            }
-            if (badr) {
-                emax = (unsigned long long)__double_as_longlong(1.0);
-                flags |= SF_ROUND_RANGE;
-            }
-        }
         // the top digit from CTA 0 (set by this squaring's fix-up, before the hand-overs)
         long long top;
         if constexpr (CL == 1) {
@@ -260,34 +245,51 @@ __global__ void __launch_bounds__(NT, (CL == 1 && NT <= 512) ? 2 : 1)
         } else {
             top = ld_cluster_s64(mapa_shared(smem_u32(misc), 0u));
         }
-        __syncthreads();
-        // 7. Montgomery fold X^2 2^-n = H - k Lo (cross terms 2 top X at weight 2^n), in-run carry
+        const int s_ = (kexp == 0 || step >= (long long)kbits - 1)
+                           ? 1
+                           : (((kexp >> (kbits - 2 - step)) & 1ull) ? mul : 1);
         {
-            const i128 ta = (i128)top;
-            const i128 s = (kexp == 0 || step >= (long long)kbits - 1)
-                               ? (i128)1
-                               : (((kexp >> (kbits - 2 - step)) & 1ull) ? (i128)mul : (i128)1);
-            for (int lr = tid; lr < R::RUNS; lr += NT) {
-                const int q = lr / R::RPR, t8 = lr % R::RPR;
-                const int t0 = t8 * RUN;
-                const unsigned long long j0 = (unsigned long long)((int)c * R::G0 + t0) + (unsigned long long)q * F1;
-                if (j0 == 0) {
-                    const i128 pend = s * ta * ta;
-                    misc[1] = (long long)(unsigned long long)pend;
-                    misc[2] = (long long)(pend >> 64);
-                }
-                i128 carry = 0;
-#pragma unroll
-                for (int u = 0; u < RUN; ++u) {
-                    const long long* cell = reinterpret_cast<const long long*>(A + q * R::SA + t0 + u);
-                    const i128 dvu = (i128)dig[lr * RUN + u];
-                    const i128 w = s * ((i128)cell[1] + ta * dvu + ta * dvu - kk * (i128)cell[0]);
-                    carry += w;
-                    dig[lr * RUN + u] = (int)take_digit(carry, digit_width(j0 + u, n, lgM));
-                }
-                cout[2 * lr] = (long long)(unsigned long long)carry;
-                cout[2 * lr + 1] = (long long)(carry >> 64);
+            int badr = 0;
+#pragma unroll 4
+            for (int i = 0; i < R::PER; ++i) {
+                const int e = tid + i * NT, q = e / R::G0, t = e % R::G0;
+                const int j = (int)c * R::G0 + t + q * F1;
+                const double2 z = cmul(A[q * R::SA + t], CACHE ? c_wi[i < NC ? i : 0] : wi[j]);
+                const long long lo = round_track(z.x, emax, badr);
+                const long long hi = round_track(z.y, emax, badr);
+                const int dv = dig[(q * R::RPR + t / RUN) * RUN + t % RUN];
+                const i128 u = fold_term(lo, hi, dv, dv, top, top, (long long)sl.k, s_);
+                long long* cell = reinterpret_cast<long long*>(A + q * R::SA + t);
+                cell[0] = (long long)(unsigned long long)u;
+                cell[1] = (long long)(u >> 64);
             }
+            if (badr) {
+                emax = (unsigned long long)__double_as_longlong(1.0);
+                flags |= SF_ROUND_RANGE;
+            }
+        }
+        __syncthreads();
+        // 7. in-run carry over the fold terms of each run
+        for (int lr = tid; lr < R::RUNS; lr += NT) {
+            const int q = lr / R::RPR, t0 = (lr % R::RPR) * RUN;
+            const unsigned long long j0 = (unsigned long long)((int)c * R::G0 + t0) + (unsigned long long)q * F1;
+            if (j0 == 0) {
+                const i128 pend = (i128)s_ * (i128)top * (i128)top;
+                misc[1] = (long long)(unsigned long long)pend;
+                misc[2] = (long long)(pend >> 64);
+            }
+            i128 u[RUN];
+#pragma unroll
+            for (int x = 0; x < RUN; ++x) {
+                const long long* cell = reinterpret_cast<const long long*>(A + q * R::SA + t0 + x);
+                u[x] = (i128)(((unsigned __int128)(unsigned long long)cell[1] << 64) | (unsigned long long)cell[0]);
+            }
+            int nd[RUN];
+            const i128 carry = run_carry(u, j0, n, lgM, nd);
+#pragma unroll
+            for (int x = 0; x < RUN; ++x) dig[lr * RUN + x] = nd[x];
+            cout[2 * lr] = (long long)(unsigned long long)carry;
+            cout[2 * lr + 1] = (long long)(carry >> 64);
         }
         res_sync<CL>();  // carries and the pending top are visible to the next fix-up
     }

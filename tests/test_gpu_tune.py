@@ -167,13 +167,18 @@ def test_tune_set_rejects_shapes_that_are_not_compiled(pg):
 
 
 # k_resident instances (radices, CTAs per residue, threads per CTA) for lone residues
-RESIDENT_LONE = [(11, 16, 128, 16, 128), (11, 16, 128, 16, 64), (11, 32, 64, 8, 256), (11, 32, 64, 8, 128),
-                 (12, 32, 128, 16, 256), (12, 32, 128, 16, 128)]
+RESIDENT_LONE = [(9, 16, 32, 4, 128), (10, 32, 32, 4, 256), (10, 32, 32, 4, 128), (10, 16, 64, 8, 128),
+                 (11, 16, 128, 16, 128), (11, 16, 128, 16, 64), (11, 32, 64, 8, 256), (11, 32, 64, 8, 128),
+                 (12, 32, 128, 16, 256), (12, 32, 128, 16, 128), (13, 64, 128, 16, 512), (13, 64, 128, 16, 256),
+                 (14, 128, 128, 16, 1024), (14, 128, 128, 16, 512), (14, 128, 128, 16, 256)]
+# an n at each length (k = 9505): the FFT length the engine picks for it is 2^lg
+RESIDENT_N = {9: 8000, 10: 16000, 11: 32768, 12: 60000, 13: 120000, 14: 250000}
 
 
 def _resident_shape(lg, f0, f1, cl, nt):
-    return {"lg": lg, "slots": 1, "passes": 2, "f0": f0, "f1": f1, "f2": 0, "g_mid": 2, "g_inner": 2,
-            "tpb": 1, "cluster": 0, "resident": cl, "resident_threads": nt}
+    # the per-pass kernels of the shape (Gerbicz products) need an inner kernel instance
+    return {"lg": lg, "slots": 1, "passes": 2, "f0": f0, "f1": f1, "f2": 0, "g_mid": 2,
+            "g_inner": 4 if f1 == 32 else 2, "tpb": 1, "cluster": 0, "resident": cl, "resident_threads": nt}
 
 
 @pytest.mark.parametrize("lg,f0,f1,cl,nt", RESIDENT_LONE)
@@ -182,7 +187,7 @@ def test_resident_lone_residue_exact(pg, gmp, lg, f0, f1, cl, nt):
     exact after single squarings (one launch each), after a chain of 300 (one
     launch), and through the a^k powering (small-multiplier schedule) and the
     Gerbicz-checked chain whose products run on the per-pass kernels."""
-    k, n = (9505, 32768) if lg == 11 else (9505, 60000)
+    k, n = 9505, RESIDENT_N[lg]
     assert pg.pick_fft_len(k, n) == 1 << lg
     pg.tune_set(pg.TUNE_ONE, _resident_shape(lg, f0, f1, cl, nt))
     try:
@@ -219,20 +224,26 @@ def test_resident_whole_test_matches_reference(pg):
         pg.tune_clear()
 
 
-@pytest.mark.parametrize("nt", [256, 1024])
-def test_resident_batch_exact(pg, gmp, nt):
-    """Batch residues one CTA each (k_resident with clusters of one) at n = 65,536:
-    a seeded sample of the uniform workload to verdict, equal to GMP."""
+@pytest.mark.parametrize("lg,f0,f1,cl,nt,n,count", [(12, 64, 64, 1, 256, 65536, 24), (12, 64, 64, 1, 1024, 65536, 24),
+                                                     (11, 32, 64, 1, 256, 30000, 24), (13, 64, 128, 2, 512, 120000, 16),
+                                                     (14, 128, 128, 4, 512, 250000, 8)])
+def test_resident_batch_exact(pg, gmp, lg, f0, f1, cl, nt, n, count):
+    """Batch residues on k_resident (one CTA each, or two or four): seeded
+    candidates to verdict through a Gerbicz-checked batch, equal to GMP."""
     from prothlogic_gb300 import workloads
-    pg.tune_set(pg.TUNE_MANY, {"lg": 12, "slots": 2, "passes": 2, "f0": 64, "f1": 64, "f2": 0, "g_mid": 2,
-                               "g_inner": 8, "tpb": 1, "cluster": 0, "resident": 1, "resident_threads": nt})
+    pg.tune_set(pg.TUNE_MANY, {"lg": lg, "slots": 2, "passes": 2, "f0": f0, "f1": f1, "f2": 0, "g_mid": 2,
+                               "g_inner": 2, "tpb": 1, "cluster": 0, "resident": cl, "resident_threads": nt})
     try:
-        rng = random.Random(nt)
-        cands = rng.sample(workloads.uniform(count=4096), 24)
+        rng = random.Random(nt + lg)
+        if n == 65536:
+            cands = rng.sample(workloads.uniform(count=4096), count)
+        else:
+            cands = [(2 * rng.randrange(1, 50000) + 1, n) for _ in range(count)]
+        assert all(pg.pick_fft_len(k, nn) == 1 << lg for k, nn in cands)
         want = gmp.proth_tests(cands)
-        b = pg.Batch(24)
-        for i, (k, n) in enumerate(cands):
-            b.submit(k, n, i)
+        b = pg.Batch(count)
+        for i, (k, nn) in enumerate(cands):
+            b.submit(k, nn, i)
         b.run(0)
         got = {r["tag"]: r for r in b.poll()}
         b.close()
