@@ -409,6 +409,19 @@ __device__ __forceinline__ long long take_digit(i128& v, int b) {
     return lo;
 }
 
+// |v| < 2^61: the carry arithmetic of a run then fits in int64 (sums stay below
+// 2^62), and the 64-bit path below gives exactly the 128-bit path's digits.
+__device__ __forceinline__ bool fits61(i128 v) {
+    const long long lo = (long long)(unsigned long long)v;
+    return (long long)(v >> 64) == (lo >> 63) && ((lo >> 61) == 0 || (lo >> 61) == -1);
+}
+__device__ __forceinline__ long long take_digit64(long long& v, int b) {
+    long long lo = v & ((1ll << b) - 1);
+    if (lo >= (1ll << (b - 1))) lo -= (1ll << b);
+    v = (v - lo) >> b;
+    return lo;
+}
+
 // floor(a / b), b > 0.  Operands that fit in 63 bits (every k below 2^40 with the
 // usual top digits) take the 64-bit division, much cheaper than the 128-bit one
 // on the critical path of the top-digit reduction; the quotient is the same.
@@ -448,6 +461,21 @@ __device__ __forceinline__ i128 run_carry(const i128 (&u)[RUN], unsigned long lo
                                           int (&nd)[RUN]) {
     unsigned long long acc = j0 * n + ((1ull << lgM) - 1);
     unsigned long long p0 = acc >> lgM;
+    bool small = true;
+#pragma unroll
+    for (int t = 0; t < RUN; ++t) small = small && fits61(u[t]);
+    if (small) {  // |carry + u| < 2^62 throughout
+        long long c64 = 0;
+#pragma unroll
+        for (int t = 0; t < RUN; ++t) {
+            acc += n;
+            const unsigned long long p1 = acc >> lgM;
+            c64 += (long long)(unsigned long long)u[t];
+            nd[t] = (int)take_digit64(c64, (int)(p1 - p0));
+            p0 = p1;
+        }
+        return (i128)c64;
+    }
     i128 carry = 0;
 #pragma unroll
     for (int t = 0; t < RUN; ++t) {
@@ -491,6 +519,28 @@ __device__ __forceinline__ void fixup_run(int (&dv)[RUN], i128 c, unsigned long 
                                           int lgM, int& bad) {
     unsigned long long acc = j0 * n + ((1ull << lgM) - 1);  // S_j = ceil(j n / M), one add per digit
     unsigned long long p0 = acc >> lgM;
+    if (fits61(c)) {
+        long long c64 = (long long)c;
+#pragma unroll
+        for (int t = 0; t < RUN; ++t) {
+            acc += n;
+            const unsigned long long p1 = acc >> lgM;
+            const int b = (int)(p1 - p0);
+            p0 = p1;
+            if (c64 != 0) {
+                long long v = (long long)dv[t] + c64;
+                if (t < RUN - 1) {
+                    dv[t] = (int)take_digit64(v, b);
+                    c64 = v;
+                } else {
+                    if (v > (1ll << 30) || v < -(1ll << 30)) bad = 1;
+                    dv[t] = (int)v;
+                    c64 = 0;
+                }
+            }
+        }
+        return;
+    }
 #pragma unroll
     for (int t = 0; t < RUN; ++t) {
         acc += n;
