@@ -163,6 +163,30 @@ static int get_plan(int lg, Plan** out, const int* F = nullptr, int P = 0) {
         off_wf[i] = host.size();
         for (int e = 0; e < d.F[i]; ++e) host.push_back(root_of_unity((uint64_t)e, (uint64_t)d.F[i]));
     }
+    // unit IBDWT weights (M divides n): pass-0 twiddles times theta^r, theta = e^(i pi / 2M),
+    // and the per-row factors theta^(q S0), conj(theta^(q S0)) / M, from long double angles
+    const long double PI_L = 3.141592653589793238462643383279502884L;
+    const size_t off_twu = host.size();
+    {
+        const std::vector<int> perm = stage_perm(d.F[0]);
+        for (int pp = 0; pp < d.F[0]; ++pp)
+            for (int r = 0; r < d.S[0]; ++r) {
+                // exp(-2 pi i r perm / M) * exp(i pi r / 2M) = exp(i pi r (1 - 4 perm) / 2M)
+                const long double num = (long double)r * (1.0L - 4.0L * (long double)perm[pp]);
+                const long double ang = PI_L * num / (2.0L * (long double)d.M);
+                host.push_back(make_double2((double)cosl(ang), (double)sinl(ang)));
+            }
+    }
+    const size_t off_thf = host.size();
+    for (int q = 0; q < d.F[0]; ++q) {
+        const long double ang = PI_L * (long double)q * (long double)d.S[0] / (2.0L * (long double)d.M);
+        host.push_back(make_double2((double)cosl(ang), (double)sinl(ang)));
+    }
+    const size_t off_thi = host.size();
+    for (int q = 0; q < d.F[0]; ++q) {
+        const long double ang = PI_L * (long double)q * (long double)d.S[0] / (2.0L * (long double)d.M);
+        host.push_back(make_double2((double)(cosl(ang) / (long double)d.M), (double)(-sinl(ang) / (long double)d.M)));
+    }
     if (cudaMalloc(&p->mem, host.size() * sizeof(double2)) != cudaSuccess) {
         delete p;
         return PG_ENOMEM;
@@ -174,6 +198,9 @@ static int get_plan(int lg, Plan** out, const int* F = nullptr, int P = 0) {
     }
     for (int i = 0; i < d.P - 1; ++i) d.tw[i] = p->mem + off_tw[i];
     for (int i = 0; i < d.P; ++i) d.wF[i] = p->mem + off_wf[i];
+    d.twu = p->mem + off_twu;
+    d.thf = p->mem + off_thf;
+    d.thi = p->mem + off_thi;
     // CTA shapes: "small" for few slots (more, smaller CTAs), "big" for batches
     const int Fl = d.F[d.P - 1];
     p->Ginner_small = (Fl == 16) ? 8 : (Fl == 32) ? 4 : 2;

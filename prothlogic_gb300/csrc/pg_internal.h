@@ -71,7 +71,17 @@ struct PlanDev {
     int Mi[MAX_PASSES];       // sub-transform length entering pass i
     const double2* tw[MAX_PASSES];   // inter-pass twiddles, tw[i][p*S[i] + r], i < P-1
     const double2* wF[MAX_PASSES];   // omega_{F[i]}^e, e < F[i]
+    // When M divides n every IBDWT weight a_j is 1 and the weight of digit
+    // j = r + q*S[0] is theta^j = theta^r theta^(q S[0]): theta^r commutes with the
+    // pass-0 transform over q and is folded into its twiddles, so only an F[0]-entry
+    // table remains (no M-entry weight tables are read).
+    const double2* twu;              // tw[0][p*S[0] + r] * theta^r
+    const double2* thf;              // theta^(q S[0]), q < F[0]
+    const double2* thi;              // conj(theta^(q S[0])) / M
 };
+
+// Whether digit weights reduce to theta^j for n (M = 2^lgM divides n).
+__host__ __device__ inline bool unit_weights(unsigned n, int lgM) { return (n & ((1u << lgM) - 1)) == 0; }
 
 }  // namespace pg
 

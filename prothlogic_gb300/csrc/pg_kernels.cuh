@@ -603,13 +603,14 @@ __device__ __forceinline__ void tile_first(const Slot& sl, const PlanDev& pl, in
     const double2* __restrict__ tw = pl.tw[0];
     double2 cw[PER], ct[PER];  // constants, loaded before waiting on the previous kernel
     const bool bound = sl.wf != nullptr;  // slots of a batch pool may not hold a candidate yet
+    const bool unit = unit_weights(sl.n, pl.lgM);
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
         const int e = tid + i * NT;
         if (e < F0 * G && bound) {
             const int q = e / G, t = e % G;
-            cw[i] = sl.wf[r0 + t + q * S0];
-            ct[i] = tw[q * S0 + r0 + t];
+            cw[i] = unit ? pl.thf[q] : sl.wf[r0 + t + q * S0];
+            ct[i] = unit ? pl.twu[q * S0 + r0 + t] : tw[q * S0 + r0 + t];
         }
     }
     if (!pre()) return;
@@ -845,13 +846,14 @@ __device__ __forceinline__ void tile_last(const Slot& sl, const Slot& pb, const 
     const double2* __restrict__ tw = pl.tw[0];
     double2 ct[PER], cw[PER];
     const bool bound = sl.wi != nullptr;  // slots of a batch pool may not hold a candidate yet
+    const bool unit = unit_weights(sl.n, pl.lgM);
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
         const int e = tid + i * NT;
         if (e < F0 * G && bound) {
             const int q = e / G, t = e % G;
-            ct[i] = tw[q * S0 + r0 + t];
-            cw[i] = sl.wi[r0 + t + q * S0];
+            ct[i] = unit ? pl.twu[q * S0 + r0 + t] : tw[q * S0 + r0 + t];
+            cw[i] = unit ? pl.thi[q] : sl.wi[r0 + t + q * S0];
         }
     }
     if (!pre()) return;
@@ -1078,14 +1080,15 @@ __global__ void __launch_bounds__(2 * F0 * TPB) k_edge(const PlanDev pl, const S
     const long long nruns = pl.M / RUN;
     const double2* __restrict__ tw = pl.tw[0];
     double2 ct[PER], cwi[PER], cwf[PER];  // constants, loaded before waiting on the previous kernel
+    const bool unit = unit_weights(sl.n, pl.lgM);
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
         const int e = tid + i * NT;
         if (e < F0 * G) {
             const int q = e / G, t = e % G;
-            ct[i] = tw[q * S0 + r0 + t];
-            cwi[i] = sl.wi[r0 + t + q * S0];
-            cwf[i] = sl.wf[r0 + t + q * S0];
+            ct[i] = unit ? pl.twu[q * S0 + r0 + t] : tw[q * S0 + r0 + t];
+            cwi[i] = unit ? pl.thi[q] : sl.wi[r0 + t + q * S0];
+            cwf[i] = unit ? pl.thf[q] : sl.wf[r0 + t + q * S0];
         }
     }
     pdl_wait();

@@ -108,7 +108,9 @@ __global__ void __launch_bounds__(NT, (CL == 1 && NT <= 512) ? 2 : 1)
     const unsigned n = sl.n;
     const int lgM = pl.lgM;
     const i128 kk = (i128)sl.k;  // the top-digit reduction
-    const double2* __restrict__ tw = pl.tw[0];
+    // n divisible by M: weights theta^(q F1) per row, theta^r folded into the twiddles
+    const bool unit = unit_weights(n, lgM);
+    const double2* __restrict__ tw = unit ? pl.twu : pl.tw[0];
     const double2* __restrict__ wf = sl.wf;
     const double2* __restrict__ wi = sl.wi;
     // With few points per thread, the weights and twiddles a thread uses stay in
@@ -121,8 +123,8 @@ __global__ void __launch_bounds__(NT, (CL == 1 && NT <= 512) ? 2 : 1)
         for (int i = 0; i < R::PER; ++i) {
             const int e = tid + i * NT, q = e / R::G0, t = e % R::G0;
             const int j = (int)c * R::G0 + t + q * F1;
-            c_wf[i] = wf[j];
-            c_wi[i] = wi[j];
+            c_wf[i] = unit ? pl.thf[q] : wf[j];
+            c_wi[i] = unit ? pl.thi[q] : wi[j];
             c_tf[i] = tw[q * F1 + (int)c * R::G0 + t];
             const int g = e / F1, x = e % F1;
             c_ti[i] = tw[((int)c * R::G1 + g) * F1 + x];
@@ -192,7 +194,7 @@ __global__ void __launch_bounds__(NT, (CL == 1 && NT <= 512) ? 2 : 1)
             const int e = tid + i * NT, q = e / R::G0, t = e % R::G0;
             const int j = (int)c * R::G0 + t + q * F1;
             const double d = (double)dig[(q * R::RPR + t / RUN) * RUN + t % RUN];
-            const double2 w = CACHE ? c_wf[i < NC ? i : 0] : wf[j];
+            const double2 w = CACHE ? c_wf[i < NC ? i : 0] : (unit ? pl.thf[q] : wf[j]);
             A[q * R::SA + t] = make_double2(d * w.x, d * w.y);
         }
         __syncthreads();
@@ -254,7 +256,7 @@ __global__ void __launch_bounds__(NT, (CL == 1 && NT <= 512) ? 2 : 1)
             for (int i = 0; i < R::PER; ++i) {
                 const int e = tid + i * NT, q = e / R::G0, t = e % R::G0;
                 const int j = (int)c * R::G0 + t + q * F1;
-                const double2 z = cmul(A[q * R::SA + t], CACHE ? c_wi[i < NC ? i : 0] : wi[j]);
+                const double2 z = cmul(A[q * R::SA + t], CACHE ? c_wi[i < NC ? i : 0] : (unit ? pl.thi[q] : wi[j]));
                 const long long lo = round_track(z.x, emax, badr);
                 const long long hi = round_track(z.y, emax, badr);
                 const int dv = dig[(q * R::RPR + t / RUN) * RUN + t % RUN];

@@ -226,7 +226,7 @@ def test_resident_whole_test_matches_reference(pg):
 
 @pytest.mark.parametrize("lg,f0,f1,cl,nt,n,count", [(12, 64, 64, 1, 256, 65536, 24), (12, 64, 64, 1, 1024, 65536, 24),
                                                      (11, 32, 64, 1, 256, 30000, 24), (13, 64, 128, 2, 512, 120000, 16),
-                                                     (14, 128, 128, 4, 512, 250000, 8)])
+                                                     (14, 128, 128, 4, 512, 170000, 6)])
 def test_resident_batch_exact(pg, gmp, lg, f0, f1, cl, nt, n, count):
     """Batch residues on k_resident (one CTA each, or two or four): seeded
     candidates to verdict through a Gerbicz-checked batch, equal to GMP."""
