@@ -180,7 +180,7 @@ int pg_prefilter(const uint64_t* ks, const uint32_t* ns, size_t count, uint64_t 
  * array's device address is looked up once per device: after cudaDeviceReset
  * the library must be reloaded before this is called again. */
 #define PG_PREFILTER_NOALLOC_MAX_COUNT 65536
-#define PG_PREFILTER_NOALLOC_SCRATCH_BYTES 2654464
+#define PG_PREFILTER_NOALLOC_SCRATCH_BYTES 557312
 int pg_prefilter_noalloc(const uint64_t* d_ks, const uint32_t* d_ns, size_t count, uint64_t bound,
                          uint64_t* d_smallest_factor, void* stream);
 

@@ -326,6 +326,16 @@ struct Pool {
 
 static const int GSTEPS = 50;  // steps per captured graph
 
+// Streams of engines and batch classes run at the device's highest priority: the
+// squaring chains are latency-bound, and side work the caller queues beside them
+// on default-priority streams (the serving loop's trial division) then only takes
+// SM slots the chains leave free.
+static cudaError_t make_stream(cudaStream_t* s) {
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) greatest = 0;
+    return cudaStreamCreateWithPriority(s, cudaStreamNonBlocking, greatest);
+}
+
 // Launch with programmatic dependent launch: the kernel's prologue (constant
 // loads) overlaps the previous kernel's tail; it waits in griddepcontrol.wait.
 static bool use_pdl() {
@@ -742,7 +752,7 @@ static int pool_create(int lg, int S, Pool** out, int mode = 0, const Shape* sha
     p->hslots.resize(S);
     p->slot_n.assign(S, 0);
     const size_t M = p->M, nruns = M / RUN;
-    bool ok = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) == cudaSuccess &&
+    bool ok = make_stream(&p->stream) == cudaSuccess &&
               cudaMalloc(&p->digits, S * M * sizeof(int)) == cudaSuccess &&
               cudaMalloc(&p->carries, S * nruns * 2 * sizeof(long long)) == cudaSuccess &&
               cudaMalloc(&p->spec, S * M * sizeof(double2)) == cudaSuccess &&
@@ -991,7 +1001,7 @@ static int solo_graph(Pool* p, int base, cudaGraphExec_t* out) {
 // ordered after both chains.
 static int pool_run_pair(Pool* p, long long steps, int a) {
     if (pool_res(p, 2)) return pool_run_sq(p, steps, false, a, 2);  // two clusters of one launch
-    if (!p->stream2) PG_CK(cudaStreamCreateWithFlags(&p->stream2, cudaStreamNonBlocking));
+    if (!p->stream2) PG_CK(make_stream(&p->stream2));
     cudaGraphExec_t ga = nullptr, gb = nullptr;
     if (steps >= GSTEPS) {
         int rc = solo_graph(p, a, &ga);

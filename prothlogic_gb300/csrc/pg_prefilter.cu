@@ -262,28 +262,29 @@ extern "C" int pg_prefilter(const uint64_t* ks, const uint32_t* ns, size_t count
 // allocation in the process, or a latency-bound serving loop in which
 // cudaMalloc/cudaFree would synchronise the device and stall the work queued on
 // other streams.  They hand in device buffers for the candidates and for the
-// result; everything else the pre-filter needs (the base primes, one segment's
-// prime list, two live-candidate lists and their counters) lives in one
-// file-scope device array of fixed size.  Every GPU on which this library is
+// result; everything else the pre-filter needs (the base primes, two
+// live-candidate lists and their counters) lives in one file-scope device array
+// of fixed size.  Every GPU on which this library is
 // loaded holds that array until the process exits.
 //
-// The kernels are the same sieve and the same test as pg_prefilter: the
-// candidates are ranked by n on the device once per call (so each prime walks
-// them with small exponent steps, as k_test does), and the live list is
-// compacted on the device in order, so one call is a fixed sequence of
-// launches on the caller's stream with no host synchronisation.  Once every
-// candidate has a factor, the remaining launches return at once.
+// One fused kernel does the work of pg_prefilter's sieve and test: each CTA
+// sieves its own window of numbers in shared memory (as k_sieve does) and tests
+// the window's primes against the live candidates right there, walking them in n
+// order (as k_test does: the candidates are ranked by n on the device once per
+// call), so no prime list is ever written to memory and a bound of 2^32 takes 32
+// launches.  The live list is compacted on the device in order after each
+// launch, so one call is a fixed sequence of launches on the caller's stream
+// with no host synchronisation; once every candidate has a factor the remaining
+// launches return at once.
 namespace pgpf {
 
-constexpr unsigned long long kNaSegNumbers = 1ull << 22;        // numbers per sieve launch
-constexpr unsigned kNaPrimeCap = (unsigned)(kNaSegNumbers / 8);  // 2^19 > pi(2^22) = 295,947
-constexpr unsigned kNaBaseCap = 8192;                            // 6,541 odd primes < 2^16
+constexpr unsigned long long kNaSegNumbers = 1ull << 27;  // numbers per launch: 256 windows of 2^19
+constexpr unsigned kNaBaseCap = 8192;                      // 6,541 odd primes < 2^16
 constexpr unsigned kNaMaxCount = PG_PREFILTER_NOALLOC_MAX_COUNT;
-// Word offsets: counters (segment primes, live count of list 0, of list 1),
-// base primes, segment primes, live list 0, live list 1.
+// Word offsets: counters (unused, live count of list 0, of list 1), base primes,
+// live list 0, live list 1.
 constexpr size_t kNaOffBase = 64;
-constexpr size_t kNaOffPrimes = kNaOffBase + kNaBaseCap;
-constexpr size_t kNaOffLive0 = kNaOffPrimes + kNaPrimeCap;
+constexpr size_t kNaOffLive0 = kNaOffBase + kNaBaseCap;
 constexpr size_t kNaOffLive1 = kNaOffLive0 + kNaMaxCount;
 constexpr size_t kNaWords = kNaOffLive1 + kNaMaxCount;
 constexpr int kNaRankThreads = 1024;
@@ -320,30 +321,65 @@ __global__ void __launch_bounds__(kNaRankThreads) k_na_seed(const uint32_t* __re
     }
 }
 
-// One thread per prime of the segment, walking the live candidates in n order:
-// 2^{n_i} mod p advances by 2^{n_i - n_{i-1}} (the walk of k_test).
-__global__ void k_na_test(const uint32_t* __restrict__ primes, const uint32_t* __restrict__ nprimes,
-                          const unsigned long long* __restrict__ ks, const uint32_t* __restrict__ ns,
-                          const uint32_t* __restrict__ live, const uint32_t* __restrict__ nlive,
-                          unsigned long long* __restrict__ factor) {
+// CTA b: the window [lo + b 2^19, lo + (b+1) 2^19) of numbers below `limit`.
+// Sieve its odd numbers with the base primes (bit set = composite), then each
+// thread takes the primes of its bitmap words and walks the live candidates in
+// n order: 2^{n_i} mod p advances by 2^{n_i - n_{i-1}}, and p | k_i 2^{n_i} + 1
+// iff k_i 2^{n_i} = -1 (mod p).
+__global__ void __launch_bounds__(kSieveThreads) k_na_sieve_test(unsigned long long lo,
+                                                                 const uint32_t* __restrict__ base, int nbase,
+                                                                 unsigned long long limit,
+                                                                 const unsigned long long* __restrict__ ks,
+                                                                 const uint32_t* __restrict__ ns,
+                                                                 const uint32_t* __restrict__ live,
+                                                                 const uint32_t* __restrict__ nlive,
+                                                                 unsigned long long* __restrict__ factor) {
+    __shared__ uint32_t bits[kSubWords];
     const unsigned nl = *nlive;
-    if (nl == 0u) return;
-    const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned np = min(*nprimes, kNaPrimeCap);
-    if (idx >= np) return;
-    const uint32_t p = primes[idx];
-    if (p < 3) return;
-    const Mont M = make_mont(p);
-    const uint32_t minus1 = p - 1;
-    uint32_t prev_n = 0;
-    uint32_t pw = mmul(1u, M.r2, M);  // 2^0 in Montgomery form
-    for (unsigned j = 0; j < nl; ++j) {
-        const uint32_t i = live[j];
-        const uint32_t n = ns[i];
-        pw = mmul(pw, mpow2(n - prev_n, M), M);
-        prev_n = n;
-        const uint32_t km = (uint32_t)(ks[i] % p);
-        if (mmul(km, pw, M) == minus1) atomicMin(&factor[i], (unsigned long long)p);
+    const unsigned long long c_lo = lo + 2ull * kSubBits * blockIdx.x;  // even
+    if (nl == 0u || c_lo >= limit) return;                               // the same in every thread
+    for (int w = threadIdx.x; w < kSubWords; w += blockDim.x) bits[w] = 0u;
+    __syncthreads();
+    const unsigned long long c_hi = c_lo + 2ull * kSubBits;  // numbers < c_hi
+    for (int i = threadIdx.x; i < nbase; i += blockDim.x) {
+        const unsigned long long q = base[i];
+        if (q * q >= c_hi) break;  // base is ascending
+        unsigned long long m = q * q;  // first odd multiple of q that is >= max(q^2, c_lo + 1)
+        if (m < c_lo + 1) {
+            m = ((c_lo + 1 + q - 1) / q) * q;
+            if (!(m & 1ull)) m += q;
+        }
+        for (; m < c_hi; m += 2 * q) {
+            const unsigned b = (unsigned)((m - c_lo - 1) >> 1);
+            atomicOr(&bits[b >> 5], 1u << (b & 31));
+        }
+    }
+    __syncthreads();
+    for (int w = threadIdx.x; w < kSubWords; w += blockDim.x) {
+        uint32_t free_bits = ~bits[w];
+        const unsigned long long first = c_lo + 1 + 64ull * w;
+        if (first == 1) free_bits &= ~1u;  // 1 is not a prime
+        if (first + 62 >= limit) {
+            for (int t = 0; t < 32; ++t)
+                if (first + 2ull * t >= limit) free_bits &= ~(1u << t);
+        }
+        while (free_bits) {
+            const int t = __ffs(free_bits) - 1;
+            free_bits &= free_bits - 1;
+            const uint32_t p = (uint32_t)(first + 2ull * t);
+            const Mont M = make_mont(p);
+            const uint32_t minus1 = p - 1;
+            uint32_t prev_n = 0;
+            uint32_t pw = mmul(1u, M.r2, M);  // 2^0 in Montgomery form
+            for (unsigned j = 0; j < nl; ++j) {
+                const uint32_t i = live[j];
+                const uint32_t n = ns[i];
+                pw = mmul(pw, mpow2(n - prev_n, M), M);
+                prev_n = n;
+                const uint32_t km = (uint32_t)(ks[i] % p);
+                if (mmul(km, pw, M) == minus1) atomicMin(&factor[i], (unsigned long long)p);
+            }
+        }
     }
 }
 
@@ -447,7 +483,6 @@ extern "C" int pg_prefilter_noalloc(const uint64_t* d_ks, const uint32_t* d_ns, 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     uint32_t* ctrl = s;
     uint32_t* live[2] = {s + kNaOffLive0, s + kNaOffLive1};
-    uint32_t* primes = s + kNaOffPrimes;
     const unsigned long long* ks = reinterpret_cast<const unsigned long long*>(d_ks);
     unsigned long long* fac = reinterpret_cast<unsigned long long*>(d_smallest_factor);
     const unsigned cnt = (unsigned)count;
@@ -456,12 +491,10 @@ extern "C" int pg_prefilter_noalloc(const uint64_t* d_ks, const uint32_t* d_ns, 
                                                                                         fac);
     int cur = 0;
     for (unsigned long long lo = 0; lo < bound; lo += kNaSegNumbers) {
-        if (cudaMemsetAsync(ctrl, 0, sizeof(uint32_t), st) != cudaSuccess) return PG_ECUDA;
         const unsigned long long limit = std::min<unsigned long long>(bound, lo + kNaSegNumbers);
         const int ctas = (int)((limit - lo + 2ull * kSubBits - 1) / (2ull * kSubBits));
-        k_sieve<<<ctas, kSieveThreads, 0, st>>>(lo, s + kNaOffBase, (int)g_na_nbase, limit, primes, ctrl,
-                                                kNaPrimeCap, ctrl + 1 + cur);
-        k_na_test<<<kNaPrimeCap / 256, 256, 0, st>>>(primes, ctrl, ks, d_ns, live[cur], ctrl + 1 + cur, fac);
+        k_na_sieve_test<<<ctas, kSieveThreads, 0, st>>>(lo, s + kNaOffBase, (int)g_na_nbase, limit, ks, d_ns,
+                                                        live[cur], ctrl + 1 + cur, fac);
         k_na_compact<<<1, kNaCompactThreads, 0, st>>>(live[cur], ctrl + 1 + cur, fac, live[cur ^ 1],
                                                       ctrl + 1 + (cur ^ 1));
         cur ^= 1;

@@ -28,8 +28,8 @@ def _random(seed, count):
 
 def _with_factor_above_segment(seed, count):
     """k*2^n+1 divisible by a prime p in (2^22, 2^23): about one in eight of
-    these has p as its smallest factor, so the live list survives several
-    2^22-number segments before the factor is found."""
+    these has p as its smallest factor, so the live list carries such candidates
+    past the smallest primes before the factor is found."""
     rng = random.Random(seed)
     out = []
     while len(out) < count:
