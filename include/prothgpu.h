@@ -184,6 +184,29 @@ int pg_prefilter(const uint64_t* ks, const uint32_t* ns, size_t count, uint64_t 
 int pg_prefilter_noalloc(const uint64_t* d_ks, const uint32_t* d_ns, size_t count, uint64_t bound,
                          uint64_t* d_smallest_factor, void* stream);
 
+/* Same answer again, for a caller that pre-filters a few candidates at a time,
+ * many times a second (a serving loop).  The reference keeps its sieve state on
+ * the device between batches of primes (init_sparse_gpu_sieve /
+ * process_sparse_prime_batch_gpu_from_vram / finalize_sparse_gpu_sieve,
+ * prothlogic4.2/gpu_engine.cu:404-450); a pg_sieve keeps every odd prime below
+ * `bound` (<= 2^32) in device memory instead, sieved once by pg_sieve_create
+ * (synchronous, allocates 8 bytes a prime: 1.6 GB at 2^32, plus 4 bytes per
+ * candidate of max_count for the live lists; make it before any stream
+ * capture, on the device it will serve).  pg_sieve_strike then queues only the
+ * trial division on `stream` (a cudaStream_t; NULL = the legacy default
+ * stream) and returns without waiting: no allocation, no host synchronisation.
+ * d_ks, d_ns and d_smallest_factor are DEVICE pointers owned by the caller;
+ * count > max_count is rejected with PG_ETOOBIG.  Strikes on one pg_sieve share
+ * its live lists: order them on the GPU (one stream, or events).
+ * pg_sieve_primes reports the number of primes held. */
+#define PG_SIEVE_MAX_COUNT 65536
+typedef struct pg_sieve pg_sieve;
+int pg_sieve_create(uint64_t bound, size_t max_count, pg_sieve** out);
+int pg_sieve_strike(pg_sieve* s, const uint64_t* d_ks, const uint32_t* d_ns, size_t count,
+                    uint64_t* d_smallest_factor, void* stream);
+int pg_sieve_primes(const pg_sieve* s, uint64_t* count);
+int pg_sieve_destroy(pg_sieve* s);
+
 /* ---- batched engine: many candidates per launch, grouped by FFT length ----
  * Replaces the reference's worker pool (dcore.cpp:84-193 dispatch with
  * worker.cpp:27-69 run_task_with_ctx over PROTH_FF_BATCH k lists). */

@@ -100,6 +100,10 @@ SIGNATURES = {
     "pg_proth_test": (ctypes.c_int, [_u64, _u32, _u32, ctypes.POINTER(PgResult)]),
     "pg_prefilter": (ctypes.c_int, [ctypes.POINTER(_u64), ctypes.POINTER(_u32), _sz, _u64, ctypes.POINTER(_u64)]),
     "pg_prefilter_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _sz, _u64, ctypes.c_void_p, ctypes.c_void_p]),
+    "pg_sieve_create": (ctypes.c_int, [_u64, _sz, ctypes.POINTER(_vp)]),
+    "pg_sieve_strike": (ctypes.c_int, [_vp, ctypes.c_void_p, ctypes.c_void_p, _sz, ctypes.c_void_p, ctypes.c_void_p]),
+    "pg_sieve_primes": (ctypes.c_int, [_vp, ctypes.POINTER(_u64)]),
+    "pg_sieve_destroy": (ctypes.c_int, [_vp]),
     "pg_batch_create": (ctypes.c_int, [_u32, _u32, ctypes.POINTER(_vp)]),
     "pg_batch_destroy": (ctypes.c_int, [_vp]),
     "pg_batch_submit": (ctypes.c_int, [_vp, _u64, _u32, _u64]),
@@ -180,22 +184,62 @@ def prefilter(cands, bound=1 << 32):
 
 
 PREFILTER_NOALLOC_MAX_COUNT = 65536
+SIEVE_MAX_COUNT = 65536
+
+
+class Sieve:
+    """Every odd prime below `bound` held in device memory (pg_sieve_create:
+    sieved once, 8 bytes a prime), for trial division of up to `max_count`
+    candidates per strike.  strike() queues the division on a CUDA stream and
+    returns at once (no allocation, no host synchronisation)."""
+
+    def __init__(self, bound=1 << 32, max_count=SIEVE_MAX_COUNT):
+        self.bound = int(bound)
+        self.max_count = int(max_count)
+        self._h = _vp()
+        _check(load().pg_sieve_create(self.bound, self.max_count, ctypes.byref(self._h)), "pg_sieve_create")
+
+    def primes(self):
+        c = _u64()
+        _check(load().pg_sieve_primes(self._h, ctypes.byref(c)), "pg_sieve_primes")
+        return int(c.value)
+
+    def strike(self, d_ks, d_ns, count, d_factor, stream):
+        """d_ks / d_ns / d_factor: device addresses (int64, int32, int64 arrays);
+        stream: a cudaStream_t value (0: the legacy default stream)."""
+        _check(load().pg_sieve_strike(self._h, ctypes.c_void_p(d_ks), ctypes.c_void_p(d_ns), count,
+                                      ctypes.c_void_p(d_factor), ctypes.c_void_p(stream)), "pg_sieve_strike")
+
+    def close(self):
+        if self._h:
+            load().pg_sieve_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class PrefilterStream:
-    """pg_prefilter_noalloc queued on a CUDA stream of its own, so trial division
-    of newly arrived candidates runs on the GPU beside the batch instead of
-    between its slices.  The device and pinned host buffers are allocated once
-    here (torch provides them and the stream); each call copies the candidates
-    in, queues the pre-filter and the copy of its answers back, and returns at
-    once; poll() hands the answers over when the work has finished.  One call at
-    a time (the pre-filter's device scratch is shared by all calls)."""
+    """Trial division of newly arrived candidates queued on a CUDA stream of its
+    own, so it runs on the GPU beside the batch instead of between its slices.
+    resident=True (the default): a Sieve made here holds the primes below the
+    bound in device memory and each call only divides; resident=False:
+    pg_prefilter_noalloc, which sieves again in every call and allocates
+    nothing.  The device and pinned host buffers are allocated once here (torch
+    provides them and the stream); each call copies the candidates in, queues
+    the division and the copy of its answers back, and returns at once; poll()
+    hands the answers over when the work has finished.  One call at a time (the
+    calls share the sieve's or the pre-filter's device scratch)."""
 
-    def __init__(self, bound=1 << 32, cap=PREFILTER_NOALLOC_MAX_COUNT):
+    def __init__(self, bound=1 << 32, cap=PREFILTER_NOALLOC_MAX_COUNT, resident=True):
         import torch
         self._torch = torch
         self.bound = int(bound)
         self.cap = int(cap)
+        self.sieve = Sieve(self.bound, self.cap) if resident else None
         self.stream = torch.cuda.Stream()
         self.h_k = torch.empty(self.cap, dtype=torch.int64, pin_memory=True)
         self.h_n = torch.empty(self.cap, dtype=torch.int32, pin_memory=True)
@@ -205,7 +249,8 @@ class PrefilterStream:
         self.d_f = torch.empty(self.cap, dtype=torch.int64, device="cuda")
         self._count = None
         self._event = None
-        # the first call on a device sets the scratch up, synchronously: do it now
+        # the first noalloc call on a device sets its scratch up, synchronously:
+        # do it now (and warm the strike path the same way)
         self.start([(3, 2048)])
         self._event.synchronize()
         self.poll()
@@ -225,9 +270,13 @@ class PrefilterStream:
         with torch.cuda.stream(self.stream):
             self.d_k[:m].copy_(self.h_k[:m], non_blocking=True)
             self.d_n[:m].copy_(self.h_n[:m], non_blocking=True)
-            _check(load().pg_prefilter_noalloc(self.d_k.data_ptr(), self.d_n.data_ptr(), m, self.bound,
-                                               self.d_f.data_ptr(), self.stream.cuda_stream),
-                   "pg_prefilter_noalloc")
+            if self.sieve is not None:
+                self.sieve.strike(self.d_k.data_ptr(), self.d_n.data_ptr(), m, self.d_f.data_ptr(),
+                                  self.stream.cuda_stream)
+            else:
+                _check(load().pg_prefilter_noalloc(self.d_k.data_ptr(), self.d_n.data_ptr(), m, self.bound,
+                                                   self.d_f.data_ptr(), self.stream.cuda_stream),
+                       "pg_prefilter_noalloc")
             self.h_f[:m].copy_(self.d_f[:m], non_blocking=True)
             self._event = torch.cuda.Event()
             self._event.record(self.stream)
@@ -245,6 +294,8 @@ class PrefilterStream:
         if self.busy():
             self._event.synchronize()
             self._count = None
+        if self.sieve is not None:
+            self.sieve.close()
 
 
 def slot_footprint(k, n):

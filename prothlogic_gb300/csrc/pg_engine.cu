@@ -1515,7 +1515,7 @@ const char* pg_strerror(int s) {
         case PG_ENODEV: return "no sm_103 device";
         case PG_ESTATE: return "handle not ready";
         case PG_EOVERFLOW: return "digit overflow";
-        case PG_ETOOBIG: return "request exceeds the fixed scratch (pg_prefilter_noalloc: at most 65536 candidates)";
+        case PG_ETOOBIG: return "request exceeds a fixed-size buffer (pg_prefilter_noalloc: at most 65536 candidates; pg_sieve_strike: the sieve's max_count, at most 65536)";
         default: return "unknown status";
     }
 }

@@ -2,9 +2,9 @@
 
 Candidates arrive over time (seeded Poisson arrivals; n log-uniform in
 [10000, 300000], k odd in [3, 10^5)).  On arrival they are trial-divided on the
-GPU by every prime below 2^32 (pg_prefilter_noalloc, queued on a stream of its
-own beside the batch, so the division overlaps the squaring work instead of
-pausing it); survivors are submitted to the batched engine (pg_batch), which
+GPU by every prime below 2^32 (pg_sieve_strike against the primes a pg_sieve
+holds in device memory, queued on a stream of its own beside the batch, so the
+division overlaps the squaring work instead of pausing it); survivors are submitted to the batched engine (pg_batch), which
 admits them under an HBM budget (the per-candidate device footprint of their
 FFT length), keeps residues and their checkpoints (every 10,000 squarings) on
 the device, and returns verdicts.  Reported: p50/p99 time-to-verdict (arrival to
