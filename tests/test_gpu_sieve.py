@@ -90,17 +90,18 @@ def test_sieve_matches_trial_division_two_strikes(pg):
     try:
         assert s.primes() == 1077870  # odd primes below 2^24 (pi(2^24) = 1,077,871)
         strikes = [
-            _random(51, 200) + _planted(61, 12, (1 << 22) + 1, (1 << 22) + 5000)
-            + _planted(62, 12, (1 << 19) + 1, (1 << 19) + 3000) + [(3, 2048), (843, 120002)],
+            _random(51, 200) + _planted(61, 40, (1 << 22) + 1, (1 << 22) + 5000)
+            + _planted(62, 40, (1 << 19) + 1, (1 << 19) + 3000) + [(3, 2048), (843, 120002)],
             _planted(63, 10, (1 << 13), (1 << 13) + 200) + _random(52, 300)
-            + _planted(64, 8, (1 << 23), 1 << 24, k_bits=40) + _random(53, 30, k_max=1 << 39),
+            + _planted(64, 30, (1 << 23), 1 << 24, k_bits=40) + _random(53, 30, k_max=1 << 39),
         ]
         for cands in strikes:
             got = _strike(s, torch, cands)
             want = [_oracle.lib().ora_smallest_factor(k, n, bound) for k, n in cands]
             assert got == want
             assert got == pg.prefilter(cands, bound=bound)
-            assert sum(1 for f in got if f > (1 << 19)) >= 4
+            # smallest factors found past the 2^19 and 2^22 stage boundaries (6 and 11 of them)
+            assert sum(1 for f in got if f > (1 << 19)) >= 6
         assert sum(1 for k, _ in strikes[1] if k >= (1 << 32)) >= 30
         first = _strike(s, torch, strikes[0])
         assert first[-2:] == [19, 0]  # 19 | 3*2^2048+1; 843*2^120002+1 is prime
