@@ -135,6 +135,64 @@ def sweep(rates, window_s=30.0, drain_s=60.0, seed=5, **kw):
     return out
 
 
+def prefilter_timing(seed=5, sizes=(1, 30, 300, 3000), slice_steps=400, slice_slots=60):
+    """Host time of one pre-filter call per size, from the call to the answers
+    on the host, for the allocating pg_prefilter, pg_prefilter_noalloc and a
+    resident pg_sieve (the three must agree), then the time of one batch slice
+    alone and beside a strike of each size."""
+    from . import prefilter
+    arr = workloads.serving(max(sizes) * 2, 256, seed=seed)
+    cands = [(k, n) for _, k, n in arr]
+    big = cands[:max(sizes)]
+    out = {}
+    for m in sizes:
+        if m >= 30:
+            t = time.perf_counter()
+            prefilter(cands[:m])
+            out[f"alloc_{m}"] = time.perf_counter() - t
+    t = time.perf_counter()
+    streams = {"resident": PrefilterStream()}
+    out["resident_create"] = time.perf_counter() - t
+    streams["noalloc"] = PrefilterStream(resident=False)
+    want = prefilter(big)
+
+    def wait(pf):
+        while True:
+            r = pf.poll()
+            if r is not None:
+                return r
+            time.sleep(0.0002)
+
+    for name, pf in streams.items():
+        for m in sizes:
+            t = time.perf_counter()
+            pf.start(cands[:m])
+            wait(pf)
+            out[f"{name}_{m}"] = time.perf_counter() - t
+        pf.start(big)
+        if wait(pf) != want:
+            raise RuntimeError(f"{name} pre-filter disagrees with pg_prefilter")
+    survivors = [c for c, f in zip(big, want) if not f][:slice_slots]
+    b = Batch(1024)
+    for i, (k, n) in enumerate(survivors):
+        b.submit(k, n, i)
+    b.run(slice_steps)
+    t = time.perf_counter()
+    b.run(slice_steps)
+    out["slice_alone"] = time.perf_counter() - t
+    for name, pf in streams.items():
+        for m in (30, max(sizes)):
+            pf.start(cands[:m])
+            t = time.perf_counter()
+            b.run(slice_steps)
+            out[f"slice_with_{name}_{m}"] = time.perf_counter() - t
+            wait(pf)
+    b.close()
+    for pf in streams.values():
+        pf.close()
+    return {k: round(v, 4) for k, v in out.items()}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--rates", default="2,4,8,16,32")
@@ -142,7 +200,12 @@ def main():
     ap.add_argument("--drain", type=float, default=60.0)
     ap.add_argument("--budget-gb", type=float, default=16.0)
     ap.add_argument("--slots", type=int, default=1024)
+    ap.add_argument("--prefilter-timing", action="store_true",
+                    help="time single pre-filter calls and a batch slice beside them, then exit")
     args = ap.parse_args()
+    if args.prefilter_timing:
+        print(json.dumps(prefilter_timing()))
+        return
     rates = [float(x) for x in args.rates.split(",")]
     res = sweep(rates, window_s=args.window, drain_s=args.drain, budget_bytes=int(args.budget_gb * (1 << 30)),
                 max_slots=args.slots)
