@@ -562,17 +562,41 @@ __device__ __forceinline__ void fixup_run(int (&dv)[RUN], i128 c, unsigned long 
 }
 
 // Round x to the nearest integer (ties to even) with one FP64 add of 1.5*2^52;
-// tracks max |x - round(x)| as the bits of a non-negative double.
+// tracks max |x - round(x)| in units of 2^-52 (kErrOne = 1.0), read off the bits
+// of x with integer operations: the FP64 pipe (two lanes per clock per SM) is
+// what a squaring waits on, the integer pipes are not.  With x = +-m 2^-sh
+// (m the 53-bit significand), the distance to the nearest integer is
+// min(f, 2^sh - f) 2^-sh for f = m mod 2^sh (|x| >= 1); 2^sh - m for
+// 1/2 <= |x| < 1, and m itself below 1/2.
+constexpr unsigned long long kErrOne = 1ull << 52;
 __device__ __forceinline__ long long round_track(double x, unsigned long long& emax, int& bad) {
     const double MAGIC = 6755399441055744.0;  // 1.5 * 2^52
-    const long long bits = __double_as_longlong(x);
-    if (((bits >> 52) & 0x7FF) >= 1023 + 50) bad = 1;  // |x| >= 2^50: outside the exact range
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    if (ex >= 1023 + 50) bad = 1;  // |x| >= 2^50: outside the exact range
     const double y = x + MAGIC;
     const long long r = __double_as_longlong(y) - 0x4338000000000000LL;
-    const double e = fabs(x - (y - MAGIC));
-    const unsigned long long eb = (unsigned long long)__double_as_longlong(e);
-    emax = eb > emax ? eb : emax;
+    const unsigned long long m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = 1075 - ex;  // x = +-m 2^-sh for ex > 0
+    unsigned long long e = 0;  // zero and subnormals (below 2^-1022) count as exact
+    if (ex != 0 && sh > 0) {
+        if (sh <= 52) {
+            const unsigned long long f = m & ((1ull << sh) - 1);
+            const unsigned long long g = (1ull << sh) - f;
+            e = (f < g ? f : g) << (52 - sh);
+        } else if (sh == 53) {
+            e = ((1ull << 53) - m) >> 1;
+        } else if (sh < 116) {
+            e = m >> (sh - 52);
+        }
+    }
+    emax = e > emax ? e : emax;
     return r;
+}
+// A max |err| in units of 2^-52 as the bits of a non-negative double (their
+// order is that of the values, so atomicMax on the bits keeps the largest).
+__device__ __forceinline__ unsigned long long err_bits(unsigned long long e) {
+    return (unsigned long long)__double_as_longlong((double)e * 0x1p-52);
 }
 
 __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
@@ -891,11 +915,11 @@ __device__ __forceinline__ void tile_last(const Slot& sl, const Slot& pb, const 
         }
     }
     if (badr) {
-        emax = (unsigned long long)__double_as_longlong(1.0);
+        emax = kErrOne;
         atomicOr(&st->flags, SF_ROUND_RANGE);
     }
     emax = warp_max_u64(emax);
-    if ((tid & 31) == 0 && emax > 0) atomicMax(&st->maxerr_bits, emax);
+    if ((tid & 31) == 0 && emax > 0) atomicMax(&st->maxerr_bits, err_bits(emax));
     // the fold term of every point, by the thread that rounded it (in place of its two halves)
     const int s_ = sched_mul(st, step_ - 1);
     const long long k_ = (long long)sl.k;
@@ -1123,11 +1147,11 @@ __global__ void __launch_bounds__(2 * F0 * TPB) k_edge(const PlanDev pl, const S
         }
     }
     if (badr) {
-        emax = (unsigned long long)__double_as_longlong(1.0);
+        emax = kErrOne;
         atomicOr(&st->flags, SF_ROUND_RANGE);
     }
     emax = warp_max_u64(emax);
-    if ((tid & 31) == 0 && emax > 0) atomicMax(&st->maxerr_bits, emax);
+    if ((tid & 31) == 0 && emax > 0) atomicMax(&st->maxerr_bits, err_bits(emax));
     __syncthreads();
     int nd[RUN] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (tid < F0) {

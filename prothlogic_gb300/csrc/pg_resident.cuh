@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(NT, (CL == 1 && NT <= 512) ? 2 : 1)
                 cell[1] = (long long)(u >> 64);
             }
             if (badr) {
-                emax = (unsigned long long)__double_as_longlong(1.0);
+                emax = kErrOne;
                 flags |= SF_ROUND_RANGE;
             }
         }
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(NT, (CL == 1 && NT <= 512) ? 2 : 1)
         sl.carries[2 * (j0 / RUN) + 1] = cout[2 * lr + 1];
     }
     emax = warp_max_u64(emax);
-    if ((tid & 31) == 0 && emax > 0) atomicMax(&st->maxerr_bits, emax);
+    if ((tid & 31) == 0 && emax > 0) atomicMax(&st->maxerr_bits, err_bits(emax));
     if (flags) atomicOr(&st->flags, flags);
     if (c == 0 && tid == 0) {
         st->top = misc[0];
