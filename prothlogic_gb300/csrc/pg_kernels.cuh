@@ -126,13 +126,20 @@ __device__ __forceinline__ int tix(int g, int i) {
     return GROUP_MAJOR ? g * S + i : i * S + g;
 }
 
+__device__ __forceinline__ double2 shfl_xor_d2(double2 v, int m) {
+    return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+
 // Radix-4 stage s of the forward transform done by a PAIR of adjacent lanes:
 // lane `sub` of the pair holds inputs sub and sub+2 of the butterfly, forms
 // their sum and difference, swaps one of them with its partner (shuffle), and
-// produces outputs sub and sub+2 with their twiddles.  The operations and their
-// order are those of bfly4_fwd + cmul, so the results are bit-identical to the
-// one-thread butterfly; each lane's FP64 chain is 16 instructions instead of 28,
-// at the price of a multiplication by w^0 = 1 (exact) on lane 0.
+// produces outputs sub and sub+2 with their twiddles.  Output 0 takes no
+// twiddle, so the three products are shared out evenly: each lane multiplies
+// its output sub+2, and output 1 (lane 1's) is multiplied half on each lane,
+// lane 0 forming the real part and lane 1 the imaginary part (one shuffle of
+// the operand to lane 0, one of the real part back).  The operations are those
+// of bfly4_fwd + cmul, so the results are bit-identical to the one-thread
+// butterfly; each lane's FP64 chain is 14 instructions instead of 28.
 template <int F, int G, bool GM, int ST = 0>
 __device__ __forceinline__ void pair_stage_fwd(double2* tile, const double2* __restrict__ wF, int tid, int s) {
     const int sub = tid & 1;
@@ -154,7 +161,15 @@ __device__ __forceinline__ void pair_stage_fwd(double2* tile, const double2* __r
     double2 ob = make_double2(u.x - v.x, u.y - v.y);          // y2 | y3
     if (h > 1) {
         const int e = j * step;
-        oa = cmul(oa, wF[sub * e]);
+        const double2 w1 = wF[e];
+        const double2 nb = shfl_xor_d2(oa, 1);                 // every lane shuffles (full mask)
+        const double2 y1 = sub ? oa : nb;                      // output 1 on both lanes
+        // the two halves of cmul(y1, w1) as one instruction pair with per-lane operands:
+        // lane 0 fma(y1.x, w1.x, (-y1.y) w1.y) = Re, lane 1 fma(y1.x, w1.y, y1.y w1.x) = Im
+        // ((-a) b == -(a b) exactly, so both equal cmul's halves bit for bit)
+        const double part = fma(y1.x, sub ? w1.y : w1.x, (sub ? y1.y : -y1.y) * (sub ? w1.x : w1.y));
+        const double re = __shfl_xor_sync(0xffffffffu, part, 1);
+        if (sub) oa = make_double2(re, part);
         ob = cmul(ob, wF[(2 + sub) * e]);
     }
     tile[ia] = oa;
@@ -162,7 +177,8 @@ __device__ __forceinline__ void pair_stage_fwd(double2* tile, const double2* __r
 }
 
 // Inverse counterpart (twiddles on the inputs, then bfly4_inv), bit-identical
-// to the one-thread butterfly.
+// to the one-thread butterfly: input 0 takes no twiddle, input 1 (lane 1's) is
+// multiplied half on each lane as in the forward stage.
 template <int F, int G, bool GM, int ST = 0>
 __device__ __forceinline__ void pair_stage_inv(double2* tile, const double2* __restrict__ wF, int tid, int s) {
     const int sub = tid & 1;
@@ -176,7 +192,14 @@ __device__ __forceinline__ void pair_stage_inv(double2* tile, const double2* __r
     double2 za = tile[ia], zb = tile[ib];
     if (h > 1) {
         const int e = j * step;
-        za = cmulc(za, wF[sub * e]);
+        const double2 w1 = wF[e];
+        const double2 nb = shfl_xor_d2(za, 1);                 // every lane shuffles (full mask)
+        const double2 z1 = sub ? za : nb;                      // input 1 on both lanes
+        // the two halves of cmulc(z1, w1) as one instruction pair with per-lane operands:
+        // lane 0 fma(z1.x, w1.x, z1.y w1.y) = Re, lane 1 fma(z1.y, w1.x, (-z1.x) w1.y) = Im
+        const double part = fma(sub ? z1.y : z1.x, w1.x, (sub ? -z1.x : z1.y) * w1.y);
+        const double re = __shfl_xor_sync(0xffffffffu, part, 1);
+        if (sub) za = make_double2(re, part);
         zb = cmulc(zb, wF[(2 + sub) * e]);
     }
     const double2 p = make_double2(za.x + zb.x, za.y + zb.y);
@@ -189,9 +212,6 @@ __device__ __forceinline__ void pair_stage_inv(double2* tile, const double2* __r
     tile[ib] = make_double2(u.x - v.x, u.y - v.y);            // Z2 | Z3
 }
 
-__device__ __forceinline__ double2 shfl_xor_d2(double2 v, int m) {
-    return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
-}
 // p + q or p - q, the sign chosen per lane without a branch (p - q == p + (-q) exactly).
 __device__ __forceinline__ double add_sgn(double p, double q, bool minus) { return p + (minus ? -q : q); }
 
