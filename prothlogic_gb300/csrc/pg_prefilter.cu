@@ -17,6 +17,12 @@
 //   test:    one thread per prime, walking the live candidates sorted by n:
 //            2^{n_i} mod p is advanced by 2^{n_i - n_{i-1}} (small exponents),
 //            p | N_i  <=>  k_i 2^{n_i} = -1 (mod p), in 32-bit Montgomery form.
+//
+// Three entry points share these pieces: pg_prefilter (allocates, sieves and
+// tests segment by segment, synchronous), pg_prefilter_noalloc (fixed scratch,
+// sieve and test fused in one kernel, queued on the caller's stream) and the
+// pg_sieve handle (every prime below the bound sieved once into device memory;
+// each strike queues only the trial division, staged by prime size).
 #include <cuda_runtime.h>
 
 #include <algorithm>
