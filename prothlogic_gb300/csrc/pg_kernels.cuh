@@ -126,6 +126,14 @@ __device__ __forceinline__ int tix(int g, int i) {
     return GROUP_MAJOR ? g * S + i : i * S + g;
 }
 
+// -x by flipping the sign bit with an integer XOR (inline PTX, so the compiler
+// cannot turn it back into an FP64 negation that takes an FP64 add to materialise).
+__device__ __forceinline__ double neg_bits(double x) {
+    int hi = __double2hiint(x);
+    asm("xor.b32 %0, %0, 0x80000000;" : "+r"(hi));
+    return __hiloint2double(hi, __double2loint(x));
+}
+
 __device__ __forceinline__ double2 shfl_xor_d2(double2 v, int m) {
     return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
 }
@@ -165,9 +173,9 @@ __device__ __forceinline__ void pair_stage_fwd(double2* tile, const double2* __r
         const double2 nb = shfl_xor_d2(oa, 1);                 // every lane shuffles (full mask)
         const double2 y1 = sub ? oa : nb;                      // output 1 on both lanes
         // the two halves of cmul(y1, w1) as one instruction pair with per-lane operands:
-        // lane 0 fma(y1.x, w1.x, (-y1.y) w1.y) = Re, lane 1 fma(y1.x, w1.y, y1.y w1.x) = Im
-        // ((-a) b == -(a b) exactly, so both equal cmul's halves bit for bit)
-        const double part = fma(y1.x, sub ? w1.y : w1.x, (sub ? y1.y : -y1.y) * (sub ? w1.x : w1.y));
+        // lane 0 fma(y1.x, w1.x, y1.y (-w1.y)) = Re, lane 1 fma(y1.x, w1.y, y1.y w1.x) = Im
+        // (a (-b) == -(a b) exactly, so both equal cmul's halves bit for bit)
+        const double part = fma(y1.x, sub ? w1.y : w1.x, y1.y * (sub ? w1.x : neg_bits(w1.y)));
         const double re = __shfl_xor_sync(0xffffffffu, part, 1);
         if (sub) oa = make_double2(re, part);
         ob = cmul(ob, wF[(2 + sub) * e]);
@@ -197,7 +205,7 @@ __device__ __forceinline__ void pair_stage_inv(double2* tile, const double2* __r
         const double2 z1 = sub ? za : nb;                      // input 1 on both lanes
         // the two halves of cmulc(z1, w1) as one instruction pair with per-lane operands:
         // lane 0 fma(z1.x, w1.x, z1.y w1.y) = Re, lane 1 fma(z1.y, w1.x, (-z1.x) w1.y) = Im
-        const double part = fma(sub ? z1.y : z1.x, w1.x, (sub ? -z1.x : z1.y) * w1.y);
+        const double part = fma(sub ? z1.y : z1.x, w1.x, (sub ? neg_bits(z1.x) : z1.y) * w1.y);
         const double re = __shfl_xor_sync(0xffffffffu, part, 1);
         if (sub) za = make_double2(re, part);
         zb = cmulc(zb, wF[(2 + sub) * e]);
