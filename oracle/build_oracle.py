@@ -1,8 +1,8 @@
-"""Build the oracle (test infrastructure, the checker) into oracle/_build/.
+"""Build the oracle (test infrastructure) into oracle/_build/.
 
 Only tests/, the smoke check and bench.py's CPU legs load what this builds.
 
-  liboracle.so        the exact checker: gcc -O3, no value-changing flags.
+  liboracle.so        the exact oracle: gcc -O3, no value-changing flags.
   liboracle_bench.so  the same C restatement built with the reference's own
                       optimisation flags (SETUP:25: -O3 -march=native
                       -funroll-loops -fomit-frame-pointer -ffast-math; on

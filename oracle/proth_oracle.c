@@ -1,7 +1,7 @@
 /*
  * proth_oracle.c -- CPU oracle for the Proth modular-squaring path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker).  Only tests/, the smoke check and the
+ * TEST INFRASTRUCTURE ONLY.  Only tests/, the smoke check and the
  * CPU-baseline leg of bench.py load this library; the product never does.
  * Each function names the ProthLogic 4.2 source it restates (file:line within
  * the reference project).  Portable C11: no intrinsics, no inline assembly, so

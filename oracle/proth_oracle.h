@@ -1,7 +1,7 @@
 /*
  * proth_oracle.h -- CPU oracle for the Proth modular-squaring path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: the tests, the
+ * TEST INFRASTRUCTURE ONLY.  The tests, the
  * smoke check and the CPU-baseline leg of bench.py call it to produce the
  * expected residues and to time the reference algorithm on host cores.  The
  * product (prothlogic_gb300 / libprothgpu) never links, loads or calls it.

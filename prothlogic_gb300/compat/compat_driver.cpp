@@ -1,8 +1,8 @@
 // compat_driver.cpp -- callers written against the reference's engine API only
 // (fft_init / fft_square_karatsuba / fft_destroy and FFTContext fields), in the
 // shape of the reference's own callers, used by the tests and the bench to show
-// the shim is a drop-in on the GPU machine (where the reference sources themselves
-// are not available to compile; oracle/ref/build_ref_callers.sh links the real
+// the shim is a drop-in on machines where the reference sources themselves are
+// not available to compile (oracle/ref/build_ref_callers.sh links the real
 // callers where they are).
 //
 //   compat_driver <k> <n> <L> <steps>          x0 hex on stdin; RES64 and ctx.last_max_diff after

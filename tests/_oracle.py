@@ -14,7 +14,7 @@ _bench_lib = None
 
 
 def lib():
-    """The exact checker (oracle/_build/liboracle.so)."""
+    """The exact oracle (oracle/_build/liboracle.so)."""
     global _lib
     if _lib is None:
         _lib = _bind(ctypes.CDLL(build_oracle()))
