@@ -193,6 +193,25 @@ def prefilter_timing(seed=5, sizes=(1, 30, 300, 3000), slice_steps=400, slice_sl
     return {k: round(v, 4) for k, v in out.items()}
 
 
+def strike_target(count=3000, seed=5):
+    """One pg_sieve_strike of `count` candidates of the serving workload against
+    every prime below 2^32 (a small profiling target: the sieve's 1.6 GB table,
+    the candidates, one strike).  Returns the number the strike rejected."""
+    import torch
+    from . import Sieve
+    cands = [(k, n) for _, k, n in workloads.serving(count, 256, seed=seed)][:count]
+    sieve = Sieve(1 << 32, len(cands))
+    ks = torch.tensor([k for k, _ in cands], dtype=torch.int64, device="cuda")
+    ns = torch.tensor([n for _, n in cands], dtype=torch.int32, device="cuda")
+    out = torch.zeros(len(cands), dtype=torch.int64, device="cuda")
+    stream = torch.cuda.current_stream()
+    sieve.strike(ks.data_ptr(), ns.data_ptr(), len(cands), out.data_ptr(), stream.cuda_stream)
+    stream.synchronize()
+    rejected = int((out != 0).sum().item())
+    sieve.close()
+    return rejected
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--rates", default="2,4,8,16,32")
@@ -202,9 +221,14 @@ def main():
     ap.add_argument("--slots", type=int, default=1024)
     ap.add_argument("--prefilter-timing", action="store_true",
                     help="time single pre-filter calls and a batch slice beside them, then exit")
+    ap.add_argument("--strike-target", type=int, default=0, metavar="COUNT",
+                    help="one resident-sieve strike of COUNT candidates (a profiling target), then exit")
     args = ap.parse_args()
     if args.prefilter_timing:
         print(json.dumps(prefilter_timing()))
+        return
+    if args.strike_target:
+        print(json.dumps({"candidates": args.strike_target, "rejected": strike_target(args.strike_target)}))
         return
     rates = [float(x) for x in args.rates.split(",")]
     res = sweep(rates, window_s=args.window, drain_s=args.drain, budget_bytes=int(args.budget_gb * (1 << 30)),
